@@ -1,0 +1,377 @@
+"""Benchmark: primary rays per second of the plain per-frame render at 1080p.
+
+Workload (one step = one frame through the public render call): the
+2048 x 2048 x 256 cave scene (seed 2, fBm heightfield + 3D simplex caves,
+4 mip levels, ~8 runs per column), a seeded camera path of 1920x1080 frames
+at 90 degrees, positions uniform over the grid 10-80 voxels above the local
+ground, yaw uniform in [0, 360), pitch uniform in [-30, 30] degrees
+(|pitch| >= 1, a horizontal view puts the ray map's vanishing point at
+infinity).  Primary rays = screen pixels; the column rays and ray-buffer
+samples behind them are reported beside the metric.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is device-timed (CUDA events on the render
+stream, L2 flushed between steps); `e2e` adds, per step, the camera from
+host memory and the copy of the colour + depth result to pinned host memory.
+`--impl reference` times the reference's CPU algorithm (the oracle port of
+Render::render_line + the resolve, all host threads) on the same frames.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG_DIR = ROOT / "rle-based-voxel-raycasting_gb300"
+METRIC = "primary Mrays/s @1080p (plain per-frame launch, 2048^2 cave scene)"
+W, H = 1920, 1080
+SCENE = dict(n=2048, sy=256, seed=2, caves=True)
+
+
+def load_rle():
+    import importlib.util
+    if "rle_gb300" in sys.modules:
+        return sys.modules["rle_gb300"]
+    spec = importlib.util.spec_from_file_location("rle_gb300", PKG_DIR / "__init__.py",
+                                                  submodule_search_locations=[str(PKG_DIR)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["rle_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def scene_bytes(rle):
+    p = rle.scenegen_default(SCENE["n"], SCENE["sy"], SCENE["n"], SCENE["seed"], caves=SCENE["caves"])
+    return rle.scenegen_rle4(p)
+
+
+def poses(rle, level0, count, seed=20261203):
+    """Seeded camera path; level0 = (sx, sy, sz, uint2 table as u32 pairs, words)."""
+    sx, sy, sz, table, words = level0
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(count):
+        x, z = rng.uniform(0, sx), rng.uniform(0, sz)
+        g = rle.ground_height(table, words, sx, sy, int(x), int(z))
+        pitch = float(rng.uniform(1.0, 30.0) * rng.choice([-1.0, 1.0]))
+        cams.append(rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)),
+                               pitch, 90.0, scene_height=sy))
+    return cams
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (ValueError, KeyError):
+            pass
+    return 6800.0, "fallback"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    rle = load_rle()
+    data = scene_bytes(rle)
+    scene = rle.Scene.from_bytes(data, device=local)
+    info = scene.info()
+    table, words = scene.copy_level(0)
+    lv0 = (info.sx[0], info.sy[0], info.sz[0], table, words)
+    cams = poses(rle, lv0, args.warmup + args.steps, seed=20261203 + rank)
+    view = rle.view_params(W, H)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    ws_bytes = rle.frame_workspace_bytes(view)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    colour = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    rms = [rle.raymap_build(c, view) for c in cams]
+
+    def step(i):
+        rle.render_frame(scene, cams[i], view, ws, ws_bytes, colour, depth, None, stream=sp)
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i)
+    torch.cuda.synchronize()
+
+    # ---- device-timed plain frames (value) ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step(args.warmup + k)
+                ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    frame_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(frame_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pixels = W * H * args.steps * world
+    value = pixels / (total_ms / 1e3) / 1e6
+
+    # ---- raycast kernel alone, same frames, with work counters (roofline) ----
+    words = rle.raybuf_words(rms[0])
+    raybuf = ws[: words * 4].view(torch.int32)
+    raydepth = ws[((words * 4 + 255) // 256) * 256:][: words * 4].view(torch.float32)
+    kt = []
+    algo_bytes = []
+    cnt = torch.zeros(6, dtype=torch.int64, device="cuda")
+    for k in range(args.steps):
+        rm = rms[args.warmup + k]
+        cnt.zero_()
+        rle.render_rays(scene, rm, raybuf, raydepth, None, cnt, stream=sp)
+        torch.cuda.synchronize()
+        c = [int(v) for v in cnt.cpu()]
+        # algorithmic bytes: 8 B per column-table entry, 2 B per run header
+        # and per colour word read, 8 B (packed word + depth) per ray sample
+        algo_bytes.append(8 * c[1] + 2 * c[2] + 2 * c[5] + 8 * rm.rays * rm.samples)
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            rle.render_rays(scene, rm, raybuf, raydepth, None, None, stream=sp)
+            b.record(stream)
+        torch.cuda.synchronize()
+        kt.append(a.elapsed_time(b))
+    k_ms = sum(kt) / len(kt)
+    achieved = (sum(algo_bytes) / len(algo_bytes)) / (k_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+
+    # ---- end to end: camera from host, colour+depth back to pinned host ----
+    host_c = torch.empty(W * H, dtype=torch.int32, pin_memory=True)
+    host_d = torch.empty(W * H, dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for k in range(args.steps):
+            step(args.warmup + k)
+            host_c.copy_(colour, non_blocking=True)
+            host_d.copy_(depth, non_blocking=True)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e = W * H * args.steps / (e2e_ms / 1e3) / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(rle, data, cams[args.warmup:args.warmup + max(1, min(args.cpu_frames, args.steps))])
+
+    rays = [rms[args.warmup + k].rays for k in range(args.steps)]
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded scene and camera path)",
+        "config": {
+            "workload": "config 2: 2048x2048x256 cave scene seed 2, 1920x1080 frames, 90 deg FOV, "
+                        "poses 10-80 above ground, yaw U[0,360), pitch U[-30,30]",
+            "scene_device_bytes": int(info.device_bytes),
+            "runs_per_column": round(info.run_headers / (SCENE["n"] ** 2), 2),
+            "column_rays_per_frame": round(sum(rays) / len(rays), 1),
+            "samples_per_ray": rms[0].samples,
+            "l2": "flushed between steps (256 MiB write)",
+            "parallelism": f"replicas x{world}",
+        },
+        "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 28,
+                "d2h_bytes_per_step": W * H * 8},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "raycast_kernel", "kernel_ms": round(k_ms, 4), "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": int(sum(algo_bytes) / len(algo_bytes))},
+        "clocks": clk.summary(),
+        "wall_s_timed": round(t_wall, 3),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def cpu_baseline(rle, data, cams):
+    """The reference's algorithm on the host cores: the oracle port of
+    Render::render_line + resolve, OpenMP over column rays, all threads."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import pyoracle as po
+    po.build_oracle()
+    oscene = po.OracleScene.from_rle4(data)
+    view = rle.view_params(W, H)
+    threads = os.cpu_count() or 1
+    t = 0.0
+    for c in cams:
+        rm = rle.raymap_build(c, view)
+        t0 = time.perf_counter()
+        om = po.raymap_from_product(rm)
+        out, dep, _, _ = po.render_rays(om, oscene, nthreads=threads)
+        po.resolve(om, W, H, out, dep)
+        t += time.perf_counter() - t0
+    value = W * H * len(cams) / t / 1e6
+    return {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{len(cams)} frame(s) of the same camera path, ray map + raycast + resolve, "
+                      f"{t / len(cams) * 1e3:.1f} ms/frame"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    rle = load_rle()
+    data = scene_bytes(rle)
+    sys.path.insert(0, str(ROOT))
+    from oracle import pyoracle as po
+    po.build_oracle()
+    oscene = po.OracleScene.from_rle4(data)
+    sx, sy, sz, table, words = oscene.levels[0]
+    cams = poses(rle, (sx, sy, sz, table, words), args.warmup + args.steps)
+    view = rle.view_params(W, H)
+    threads = os.cpu_count() or 1
+
+    def frame(c):
+        rm = rle.raymap_build(c, view)
+        om = po.raymap_from_product(rm)
+        out, dep, _, _ = po.render_rays(om, oscene, nthreads=threads)
+        po.resolve(om, W, H, out, dep)
+
+    for c in cams[:args.warmup]:
+        frame(c)
+    t0 = time.perf_counter()
+    for c in cams[args.warmup:]:
+        frame(c)
+    t = time.perf_counter() - t0
+    value = W * H * args.steps / t / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and camera path)",
+        "config": {"workload": "config 2: 2048x2048x256 cave scene seed 2, 1920x1080 frames, 90 deg FOV, "
+                               "poses 10-80 above ground, yaw U[0,360), pitch U[-30,30]"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} frame(s): ray map + Render::render_line port + resolve, "
+                                   f"OpenMP over column rays"},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,230 @@
+/* rle_gb300: GB300-native (sm_103a) renderer for scenes stored as
+ * run-length-encoded voxel columns (.rle4).
+ *
+ * C ABI.  Every entry point returns an rle_status; device buffers are owned by
+ * the caller unless an entry point says otherwise; work is ordered on the
+ * CUDA stream the caller passes (a cudaStream_t passed as void*, NULL = the
+ * legacy default stream).  Handles are safe to use from several host threads
+ * as long as one handle is not freed while in use.
+ *
+ * The render path replaces the reference's
+ *   extern "C" void cuda_main_render2(int pbo_out, int width, int height,
+ *                                     RayMap_GPU* raymap)
+ * (RLE-Raycaster/src/Cuda_Main.cu:124,183-271) and the code around it:
+ *   RayMap::get_ray_map      src/RayMap.h:98-402      -> rle_raymap_build
+ *   Render::render_line      src/Cuda_Render.h:96-737 -> rle_render_rays
+ *   colorize_*.frag resolve  bin/shader/colorize_buddha_soft.frag:12-80
+ *                                                     -> rle_resolve
+ *   RLE4::load/all_to_gpu    src/Rle4.cpp:244-448     -> rle_scene_load_*
+ * The GL pixel-buffer output of the reference becomes caller-owned device
+ * buffers.
+ */
+#ifndef RLE_GB300_H
+#define RLE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rle_status {
+    RLE_OK = 0,
+    RLE_ERR_INVALID_ARG = -1, /* null pointer, bad size, non-finite camera, ... */
+    RLE_ERR_IO = -2,          /* file could not be opened or read */
+    RLE_ERR_FORMAT = -3,      /* .rle4 bytes inconsistent with their headers */
+    RLE_ERR_CUDA = -4,        /* a CUDA runtime call failed */
+    RLE_ERR_NO_MEMORY = -5,   /* host or device allocation failed / budget exceeded */
+    RLE_ERR_CAPACITY = -6,    /* output or work buffer too small, limit exceeded */
+    RLE_ERR_TIMEOUT = -7,     /* a bounded wait gave up */
+    RLE_ERR_CANCELLED = -8,   /* request cancelled before it ran */
+    RLE_ERR_UNSUPPORTED = -9  /* feature not available on this device/build */
+} rle_status;
+
+#define RLE_MAX_MIPS 8
+
+/* Printable name of a status. */
+const char* rle_status_string(rle_status s);
+/* Build identification, e.g. "rle_gb300 1.0 sm_103a". */
+const char* rle_version(void);
+/* Message of the last error on the calling host thread (may be empty). */
+const char* rle_last_error(void);
+
+/* ---------------------------------------------------------------------- */
+/* Scenes                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* A scene resident on one device: per mip level the column table
+ * (uint2 {slab_offset, run_count | first_header << 16}, one per column,
+ * x fastest) and the slab words (u16 run headers then u16 colours per
+ * column), exactly the layout RLE4::load builds (src/Rle4.cpp:285-314),
+ * with 32-bit offsets widened to unsigned (up to 2^32 words per level). */
+typedef struct rle_scene rle_scene;
+
+typedef struct rle_scene_info {
+    int device;
+    int nummaps;
+    int sx[RLE_MAX_MIPS], sy[RLE_MAX_MIPS], sz[RLE_MAX_MIPS];
+    uint64_t slab_words[RLE_MAX_MIPS];
+    uint64_t device_bytes;   /* table + slab bytes held on the device */
+    uint64_t run_headers;    /* run headers over all columns of level 0 */
+    uint64_t surface_voxels; /* colour words of level 0 */
+} rle_scene_info;
+
+/* .rle4 file or bytes (src/Rle4.cpp:220-242 format: int nummaps, then per
+ * level int sx, sy, sz, slabs_size and u16 slabs[slabs_size]).  Builds the
+ * column tables on the host and uploads to `device`.  sx and sz must be
+ * powers of two (the renderer wraps the map toroidally). */
+rle_status rle_scene_load_file(const char* path, int device, rle_scene** out);
+rle_status rle_scene_load_memory(const void* bytes, size_t nbytes, int device, rle_scene** out);
+rle_status rle_scene_free(rle_scene* scene);
+rle_status rle_scene_get_info(const rle_scene* scene, rle_scene_info* out);
+/* Host copy of one level's column table (2*sx*sz u32) and/or slab words. */
+rle_status rle_scene_copy_level(const rle_scene* scene, int mip, uint32_t* table, uint16_t* slabs);
+
+/* ---------------------------------------------------------------------- */
+/* Synthetic scenes (seeded, deterministic on every host)                 */
+/* ---------------------------------------------------------------------- */
+
+typedef struct rle_scenegen_params {
+    int sx, sy, sz;          /* grid; sx, sz powers of two >= 8; sy multiple of 64, <= 1024 */
+    uint64_t seed;
+    int nummaps;             /* mip levels, each halving x, y and z (>= 1) */
+    float height_min;        /* fBm ground height range, voxels */
+    float height_max;
+    int octaves;             /* fBm value-noise octaves */
+    int base_period;         /* lattice period of the lowest octave, voxels */
+    int caves;               /* carve 3D simplex-noise caves/overhangs */
+    float cave_y0, cave_y1;  /* height band the caves live in */
+    float cave_threshold;    /* density above which a voxel is carved */
+    float cave_period;       /* wavelength of the cave noise, voxels */
+} rle_scenegen_params;
+
+/* Defaults for a scene of the given size and seed: heights 32..224 scaled
+ * by sy/256, 6 octaves; caves (when asked) in the band 64..200 scaled. */
+rle_status rle_scenegen_default(int sx, int sy, int sz, uint64_t seed, int caves,
+                                rle_scenegen_params* out);
+/* Generates the scene and returns it as .rle4 bytes (free with rle_host_free). */
+rle_status rle_scenegen_rle4(const rle_scenegen_params* p, void** bytes, size_t* nbytes);
+/* Dense view of one mip level for small scenes: solid bits in the
+ * reference's Tree layout (bit i&7 of byte (i + j*sx + k*sx*sy) >> 3) and the
+ * RGB565 colour the generator gives every voxel (same index, no >> 3). */
+rle_status rle_scenegen_dense(const rle_scenegen_params* p, int mip, uint8_t* bits,
+                              uint16_t* colours);
+void rle_host_free(void* p);
+
+/* ---------------------------------------------------------------------- */
+/* Cameras and ray maps                                                   */
+/* ---------------------------------------------------------------------- */
+
+typedef struct rle_camera {
+    float pos[3];   /* RayMap_GPU.position: x, z on the column grid; y is
+                       minus the eye height (a voxel of height h sits at
+                       pos[1] + h relative to the eye) */
+    float rot[3];   /* RayMap_GPU.rotation: x = pitch in radians (positive
+                       looks down), y = yaw in radians, z unused */
+    float fov_deg;  /* horizontal field of view; 90 is the reference frustum */
+} rle_camera;
+
+typedef struct rle_view_params {
+    int width, height;  /* screen in pixels */
+    int samples;        /* samples per column ray (RENDER_SIZE); 0 = width */
+    int maxres;         /* column rays per unit of fan (RAYS_CASTED_RES/4); 0 = width */
+    float border;       /* vertical border of the square ray-map plane; <= 0 = (W-H)/(2W) */
+    int mip_distance;   /* distance of the first LOD switch (MIP_DISTANCE); 0 = width */
+    int z_far;          /* ray length in DDA steps (RAYS_DISTANCE); 0 = 80000 */
+} rle_view_params;
+
+/* Per-frame state of one camera: the fields of RayMap_GPU
+ * (src/RayMap.h:16-54) without the scene pointers, plus the render
+ * parameters the reference fixes at compile time and the per-frame sines
+ * and cosines the device would otherwise compute. */
+typedef struct rle_raymap {
+    float vanishing_point_2d[3];
+    int map_line_count;        /* sum of res[] */
+    float rotation[3];
+    float position[3];
+    float border, clip_min, clip_max;
+    int maxres;
+    int res[4];                /* column rays of the up, down, left, right fans */
+    float p4[3];
+    float p_2d[8][3];
+    float p_no[8][3];
+    float to3d[4][4];
+    float p_ofs_min[4], p_ofs_max[4];
+    int samples;               /* samples per ray (S) */
+    int mip_distance;
+    int z_far;
+    float fov_scale;           /* tan(fov/2) */
+    /* derived, filled by rle_raymap_build */
+    float sin_x, cos_x, sin_y, cos_y;    /* of rotation.x / rotation.y */
+    float sin_neg_y, cos_neg_y;          /* of -rotation.y */
+    int width, height;         /* screen */
+    int rows;                  /* ray-buffer rows (RAYS_CASTED = 4*maxres) */
+    int rays;                  /* rays rendered: min(map_line_count, rows) */
+} rle_raymap;
+
+/* RayMap::get_ray_map for one camera (host, microseconds). */
+rle_status rle_raymap_build(const rle_camera* cam, const rle_view_params* view, rle_raymap* out);
+
+/* ---------------------------------------------------------------------- */
+/* Rendering                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* The voxel that coloured a sample or pixel. */
+typedef struct rle_hit {
+    uint16_t x, z, y;   /* cell and height at level `mip` */
+    uint8_t mip;
+    uint8_t flags;      /* 1 = voxel, 2 = sky, 0 = no data */
+} rle_hit;
+
+/* Per-ray work counters (the reference's DETAIL_BENCH counters,
+ * src/Cuda_Render.h:14-22), summed over a frame. */
+typedef struct rle_counters {
+    unsigned long long cells;    /* DDA cells stepped */
+    unsigned long long fetched;  /* column-table entries read (8 B) */
+    unsigned long long headers;  /* run headers read from slabs (2 B) */
+    unsigned long long runs;     /* solid runs examined */
+    unsigned long long spans;    /* spans drawn */
+    unsigned long long pixels;   /* samples coloured (2 B colour read each) */
+} rle_counters;
+
+/* Words of the ray buffer of a ray map: rows * samples. */
+size_t rle_raybuf_words(const rle_raymap* rm);
+
+/* Drop-in for cuda_main_render2: casts every column ray of the ray map into
+ * the ray buffer, row r = ray r, `samples` words per row.
+ *   d_raybuf   (required) colour16 | depth16 << 16 per sample, as the PBO of
+ *              the reference; 0x00ff8844 = sky; 0 = outside the ray's range
+ *   d_raydepth (required) float depth (1/onez) per sample; +inf sky; 0 none
+ *   d_rayhit   (optional) rle_hit per sample
+ *   d_counters (optional) one rle_counters, accumulated (atomically)
+ * Rows >= rm->rays are left untouched. */
+rle_status rle_render_rays(const rle_scene* scene, const rle_raymap* rm, uint32_t* d_raybuf,
+                           float* d_raydepth, rle_hit* d_rayhit, rle_counters* d_counters,
+                           void* stream);
+
+/* The colorize shader's resolve as a kernel: per screen pixel (row 0 at the
+ * top), the ray-buffer sample its fan geometry selects.
+ *   d_colour RGBA8 (R in the low byte): RGB565 expanded, sky 0xFFFFCCB2, none 0
+ *   d_depth  float depth, +inf sky, 0 none
+ *   d_hit    (optional) the sample's rle_hit
+ * Ray-buffer rows >= rm->rays were not cast and read as no data. */
+rle_status rle_resolve(const rle_raymap* rm, const uint32_t* d_raybuf, const float* d_raydepth,
+                       const rle_hit* d_rayhit, uint32_t* d_colour, float* d_depth,
+                       rle_hit* d_hit, void* stream);
+
+/* Camera to screen in one call: ray map on the host, raycast and resolve on
+ * the device.  The ray buffer lives in d_workspace, which must hold
+ * rle_frame_workspace_bytes(view) bytes (256-byte aligned). */
+size_t rle_frame_workspace_bytes(const rle_view_params* view);
+rle_status rle_render_frame(const rle_scene* scene, const rle_camera* cam,
+                            const rle_view_params* view, void* d_workspace,
+                            size_t workspace_bytes, uint32_t* d_colour, float* d_depth,
+                            rle_hit* d_hit, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

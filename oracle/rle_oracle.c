@@ -840,6 +840,7 @@ void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const ui
     const float ofs_x = -rm->p_ofs_min[0], ofs_y = -rm->p_ofs_min[1] + ofs1;
     const float ofs_z = -rm->p_ofs_min[2] + ofs2, ofs_w = -rm->p_ofs_min[3] + ofs3;
     const float rxg0 = rm->rotation.x > 0 ? 1.0f : 0.0f;
+    const int rays = orc_rays_to_render(rm);
 
     for (int row = 0; row < height; row++)
         for (int col = 0; col < width; col++) {
@@ -875,9 +876,11 @@ void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const ui
             int r = texel(ty, rows);
             size_t si = (size_t)r * S + s;
             size_t pi = (size_t)row * width + col;
-            uint32_t w = raybuf[si];
-            if (sample_index) sample_index[pi] = (int64_t)si;
-            float d = raydepth[si];
+            /* rows past the rays cast hold no data */
+            const int cast = r < rays;
+            uint32_t w = cast ? raybuf[si] : 0u;
+            if (sample_index) sample_index[pi] = cast ? (int64_t)si : -1;
+            float d = cast ? raydepth[si] : 0.0f;
             if (((w >> 16) & 0xff) == 0xff) {
                 /* sky: the shader's c.z == 1.0 test (byte 2 of 0x00ff8844) */
                 colour[pi] = 0xffffccb2u; /* vec4(178,204,255,255)/255 */
@@ -891,7 +894,7 @@ void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const ui
                 depth[pi] = d;
             }
             if (hit) {
-                if (rayhit) hit[pi] = rayhit[si];
+                if (rayhit && cast) hit[pi] = rayhit[si];
                 else memset(&hit[pi], 0, sizeof(orc_hit));
             }
         }

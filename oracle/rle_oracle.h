@@ -116,7 +116,8 @@ int orc_render_rays(const orc_raymap* rm, const orc_mip* mips, int nummaps, int 
  * range (no data); byte 2 == 0xff marks sky, as the shader's c.z == 1.0 test.
  * colour: RGBA8 from RGB565 for hits, 0xFFFFCCB2 for sky, 0 for no data.
  * depth: the sample's float depth, +inf for sky, 0 for no data.
- * sample_index (optional): the ray-buffer word index each pixel fetched. */
+ * Rows at or past orc_rays_to_render(rm) were not cast and read as no data.
+ * sample_index (optional): the ray-buffer word index each pixel fetched (-1: none). */
 void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const uint32_t* raybuf,
                  const float* raydepth, const orc_hit* rayhit, uint32_t* colour, float* depth,
                  orc_hit* hit, int64_t* sample_index);

@@ -1,0 +1,312 @@
+"""Python mirror of the rle_gb300 C ABI (include/rle_gb300.h), over ctypes.
+
+The names, argument meaning and errors follow the C entry points, which in
+turn replace the reference's render path: ``raymap_build`` is
+RayMap::get_ray_map (src/RayMap.h:98-402), ``render_rays`` is
+cuda_main_render2 / Render::render_line (src/Cuda_Main.cu:183-271,
+src/Cuda_Render.h:96-737), ``resolve`` is the colorize shader
+(bin/shader/colorize_buddha_soft.frag:12-80) and ``Scene`` is
+RLE4::load + all_to_gpu (src/Rle4.cpp:244-448).
+
+Device buffers are passed as raw device pointers (int) or any object with a
+``data_ptr()`` method (a CUDA torch.Tensor).  The CUDA library must be built
+(``build.py``); importing without it raises ImportError -- there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+from typing import Optional
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "librle_gb300.so"
+RLE_MAX_MIPS = 8
+# rotation.x of the reference grows as the view turns down (src/RayMap.h:121);
+# camera() takes pitch with negative = down.
+PITCH_SIGN = -1.0
+
+STATUS = {
+    0: "RLE_OK", -1: "RLE_ERR_INVALID_ARG", -2: "RLE_ERR_IO", -3: "RLE_ERR_FORMAT", -4: "RLE_ERR_CUDA",
+    -5: "RLE_ERR_NO_MEMORY", -6: "RLE_ERR_CAPACITY", -7: "RLE_ERR_TIMEOUT", -8: "RLE_ERR_CANCELLED",
+    -9: "RLE_ERR_UNSUPPORTED",
+}
+
+
+class RLEError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str = ""):
+        self.status = status
+        self.name = STATUS.get(status, str(status))
+        super().__init__(f"{where}: {self.name}" + (f" ({message})" if message else ""))
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("rot", C.c_float * 3), ("fov_deg", C.c_float)]
+
+
+class ViewParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("samples", C.c_int), ("maxres", C.c_int),
+                ("border", C.c_float), ("mip_distance", C.c_int), ("z_far", C.c_int)]
+
+
+class RayMap(C.Structure):
+    _fields_ = [
+        ("vanishing_point_2d", C.c_float * 3), ("map_line_count", C.c_int), ("rotation", C.c_float * 3),
+        ("position", C.c_float * 3), ("border", C.c_float), ("clip_min", C.c_float), ("clip_max", C.c_float),
+        ("maxres", C.c_int), ("res", C.c_int * 4), ("p4", C.c_float * 3), ("p_2d", (C.c_float * 3) * 8),
+        ("p_no", (C.c_float * 3) * 8), ("to3d", (C.c_float * 4) * 4), ("p_ofs_min", C.c_float * 4),
+        ("p_ofs_max", C.c_float * 4), ("samples", C.c_int), ("mip_distance", C.c_int), ("z_far", C.c_int),
+        ("fov_scale", C.c_float), ("sin_x", C.c_float), ("cos_x", C.c_float), ("sin_y", C.c_float),
+        ("cos_y", C.c_float), ("sin_neg_y", C.c_float), ("cos_neg_y", C.c_float), ("width", C.c_int),
+        ("height", C.c_int), ("rows", C.c_int), ("rays", C.c_int),
+    ]
+
+
+class Hit(C.Structure):
+    _fields_ = [("x", C.c_uint16), ("z", C.c_uint16), ("y", C.c_uint16), ("mip", C.c_uint8), ("flags", C.c_uint8)]
+
+
+HIT_DTYPE = np.dtype([("x", "<u2"), ("z", "<u2"), ("y", "<u2"), ("mip", "u1"), ("flags", "u1")])
+COUNTER_FIELDS = ("cells", "fetched", "headers", "runs", "spans", "pixels")
+
+
+class Counters(C.Structure):
+    _fields_ = [(n, C.c_ulonglong) for n in COUNTER_FIELDS]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("device", C.c_int), ("nummaps", C.c_int), ("sx", C.c_int * RLE_MAX_MIPS),
+                ("sy", C.c_int * RLE_MAX_MIPS), ("sz", C.c_int * RLE_MAX_MIPS),
+                ("slab_words", C.c_uint64 * RLE_MAX_MIPS), ("device_bytes", C.c_uint64),
+                ("run_headers", C.c_uint64), ("surface_voxels", C.c_uint64)]
+
+
+class ScenegenParams(C.Structure):
+    _fields_ = [("sx", C.c_int), ("sy", C.c_int), ("sz", C.c_int), ("seed", C.c_uint64), ("nummaps", C.c_int),
+                ("height_min", C.c_float), ("height_max", C.c_float), ("octaves", C.c_int),
+                ("base_period", C.c_int), ("caves", C.c_int), ("cave_y0", C.c_float), ("cave_y1", C.c_float),
+                ("cave_threshold", C.c_float), ("cave_period", C.c_float)]
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built; run build.py (the renderer has no CPU fallback)")
+    lib = C.CDLL(str(LIB_PATH))
+    vp = C.c_void_p
+    sig = {
+        "rle_status_string": (C.c_char_p, [C.c_int]),
+        "rle_version": (C.c_char_p, []),
+        "rle_last_error": (C.c_char_p, []),
+        "rle_scene_load_file": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(vp)]),
+        "rle_scene_load_memory": (C.c_int, [vp, C.c_size_t, C.c_int, C.POINTER(vp)]),
+        "rle_scene_free": (C.c_int, [vp]),
+        "rle_scene_get_info": (C.c_int, [vp, C.POINTER(SceneInfo)]),
+        "rle_scene_copy_level": (C.c_int, [vp, C.c_int, vp, vp]),
+        "rle_scenegen_default": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.POINTER(ScenegenParams)]),
+        "rle_scenegen_rle4": (C.c_int, [C.POINTER(ScenegenParams), C.POINTER(vp), C.POINTER(C.c_size_t)]),
+        "rle_scenegen_dense": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, vp, vp]),
+        "rle_host_free": (None, [vp]),
+        "rle_raymap_build": (C.c_int, [C.POINTER(Camera), C.POINTER(ViewParams), C.POINTER(RayMap)]),
+        "rle_raybuf_words": (C.c_size_t, [C.POINTER(RayMap)]),
+        "rle_render_rays": (C.c_int, [vp, C.POINTER(RayMap), vp, vp, vp, vp, vp]),
+        "rle_resolve": (C.c_int, [C.POINTER(RayMap), vp, vp, vp, vp, vp, vp, vp]),
+        "rle_frame_workspace_bytes": (C.c_size_t, [C.POINTER(ViewParams)]),
+        "rle_render_frame": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, C.c_size_t, vp, vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_lib = _load()
+
+
+def library() -> C.CDLL:
+    """The loaded librle_gb300.so (for entry points without a wrapper)."""
+    return _lib
+
+
+def _check(status: int, where: str) -> None:
+    if status != 0:
+        msg = _lib.rle_last_error()
+        raise RLEError(status, where, msg.decode() if msg else "")
+
+
+def ptr(x) -> Optional[int]:
+    """Device pointer of an int, None or a tensor-like with data_ptr()."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    raise TypeError(f"cannot take a device pointer of {type(x).__name__}")
+
+
+def version() -> str:
+    return _lib.rle_version().decode()
+
+
+# ---------------------------------------------------------------------------
+# scenes
+# ---------------------------------------------------------------------------
+
+def scenegen_default(sx: int, sy: int, sz: int, seed: int, caves: bool = False) -> ScenegenParams:
+    p = ScenegenParams()
+    _check(_lib.rle_scenegen_default(sx, sy, sz, seed, int(caves), C.byref(p)), "rle_scenegen_default")
+    return p
+
+
+def scenegen_rle4(params: ScenegenParams) -> bytes:
+    """Seeded synthetic scene as .rle4 bytes."""
+    buf = C.c_void_p()
+    n = C.c_size_t()
+    _check(_lib.rle_scenegen_rle4(C.byref(params), C.byref(buf), C.byref(n)), "rle_scenegen_rle4")
+    try:
+        return C.string_at(buf, n.value)
+    finally:
+        _lib.rle_host_free(buf)
+
+
+def scenegen_dense(params: ScenegenParams, mip: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """Solid bits (Tree layout) and RGB565 colours of one level of a small scene."""
+    sx, sy, sz = params.sx >> mip, params.sy >> mip, params.sz >> mip
+    bits = np.zeros((sx * sy * sz + 7) // 8, np.uint8)
+    cols = np.zeros(sx * sy * sz, np.uint16)
+    _check(_lib.rle_scenegen_dense(C.byref(params), mip, bits.ctypes.data, cols.ctypes.data), "rle_scenegen_dense")
+    return bits, cols
+
+
+class Scene:
+    """A scene resident on one GPU (column tables + slab words per level)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def from_file(cls, path: str, device: int = 0) -> "Scene":
+        h = C.c_void_p()
+        _check(_lib.rle_scene_load_file(str(path).encode(), device, C.byref(h)), "rle_scene_load_file")
+        return cls(h)
+
+    @classmethod
+    def from_bytes(cls, data: bytes, device: int = 0) -> "Scene":
+        h = C.c_void_p()
+        buf = C.create_string_buffer(data, len(data))
+        _check(_lib.rle_scene_load_memory(buf, len(data), device, C.byref(h)), "rle_scene_load_memory")
+        return cls(h)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if not self._h:
+            raise RLEError(-1, "Scene", "scene was freed")
+        return self._h
+
+    def info(self) -> SceneInfo:
+        i = SceneInfo()
+        _check(_lib.rle_scene_get_info(self.handle, C.byref(i)), "rle_scene_get_info")
+        return i
+
+    def copy_level(self, mip: int) -> tuple[np.ndarray, np.ndarray]:
+        """Host copies of one level's uint2 table (as 2*sx*sz u32) and slab words."""
+        i = self.info()
+        table = np.zeros(2 * i.sx[mip] * i.sz[mip], np.uint32)
+        slabs = np.zeros(int(i.slab_words[mip]), np.uint16)
+        _check(_lib.rle_scene_copy_level(self.handle, mip, table.ctypes.data, slabs.ctypes.data),
+               "rle_scene_copy_level")
+        return table, slabs
+
+    def free(self) -> None:
+        if self._h:
+            _check(_lib.rle_scene_free(self._h), "rle_scene_free")
+            self._h = C.c_void_p()
+
+    def __enter__(self) -> "Scene":
+        return self
+
+    def __exit__(self, *a) -> None:
+        self.free()
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.rle_scene_free(self._h)
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# cameras and ray maps
+# ---------------------------------------------------------------------------
+
+def camera(x: float, z: float, eye_height: float, yaw_deg: float, pitch_deg: float,
+           fov_deg: float = 90.0, scene_height: int = 256) -> Camera:
+    """Camera at (x, z) on the grid, eye_height voxels above the bottom of a
+    scene scene_height voxels tall, looking along yaw; negative pitch looks
+    down.  In the reference's convention the column axis points down (word 0
+    of a column is the top) and position.y is the eye's coordinate on it,
+    negated: a voxel at index j lies j + position.y below the eye."""
+    c = Camera()
+    c.pos[:] = (x, eye_height - scene_height, z)
+    c.rot[:] = (PITCH_SIGN * math.radians(pitch_deg), math.radians(yaw_deg), 0.0)
+    c.fov_deg = fov_deg
+    return c
+
+
+def view_params(width: int, height: int, samples: int = 0, maxres: int = 0, border: float = 0.0,
+                mip_distance: int = 0, z_far: int = 0) -> ViewParams:
+    return ViewParams(width, height, samples, maxres, border, mip_distance, z_far)
+
+
+def raymap_build(cam: Camera, view: ViewParams) -> RayMap:
+    rm = RayMap()
+    _check(_lib.rle_raymap_build(C.byref(cam), C.byref(view), C.byref(rm)), "rle_raymap_build")
+    return rm
+
+
+def raybuf_words(rm: RayMap) -> int:
+    return int(_lib.rle_raybuf_words(C.byref(rm)))
+
+
+# ---------------------------------------------------------------------------
+# rendering
+# ---------------------------------------------------------------------------
+
+def render_rays(scene: Scene, rm: RayMap, raybuf, raydepth, rayhit=None, counters=None, stream: int = 0) -> None:
+    _check(_lib.rle_render_rays(scene.handle, C.byref(rm), ptr(raybuf), ptr(raydepth), ptr(rayhit),
+                                ptr(counters), stream or None), "rle_render_rays")
+
+
+def resolve(rm: RayMap, raybuf, raydepth, colour, depth, rayhit=None, hit=None, stream: int = 0) -> None:
+    _check(_lib.rle_resolve(C.byref(rm), ptr(raybuf), ptr(raydepth), ptr(rayhit), ptr(colour), ptr(depth),
+                            ptr(hit), stream or None), "rle_resolve")
+
+
+def frame_workspace_bytes(view: ViewParams) -> int:
+    return int(_lib.rle_frame_workspace_bytes(C.byref(view)))
+
+
+def render_frame(scene: Scene, cam: Camera, view: ViewParams, workspace, workspace_bytes: int, colour, depth,
+                 hit=None, stream: int = 0) -> None:
+    _check(_lib.rle_render_frame(scene.handle, C.byref(cam), C.byref(view), ptr(workspace), workspace_bytes,
+                                 ptr(colour), ptr(depth), ptr(hit), stream or None), "rle_render_frame")
+
+
+def ground_height(table: np.ndarray, slabs: np.ndarray, sx: int, sy: int, x: int, z: int) -> int:
+    """Height above the bottom of the topmost stored voxel's upper face in
+    column (x, z) of a level (0 for an empty column), from host copies of the
+    level's table and slab words.  Column words run from the top down."""
+    c = (z * sx + x) * 2
+    ofs, count = int(table[c]), int(table[c + 1]) & 0xFFFF
+    depth = 0
+    for r in range(count):
+        w = int(slabs[ofs + 2 + r])
+        depth += w & 1023
+        if w >> 10:
+            return sy - depth
+    return 0

@@ -1,0 +1,103 @@
+// Internal declarations shared by the host C++ and the CUDA translation units.
+#pragma once
+
+#include <vector_types.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "rle_gb300.h"
+
+namespace rle {
+
+// Per-thread last-error message behind rle_last_error().
+void set_error(const char* fmt, ...);
+void clear_error();
+
+// One mip level resident on the device.  The table is the uint2 column
+// directory {slab_offset, run_count | first_header << 16}, x fastest
+// (RLE4::load, src/Rle4.cpp:285-314); slabs are the u16 words.
+struct Level {
+    int sx = 0, sy = 0, sz = 0;
+    uint64_t words = 0;
+    uint32_t* d_table = nullptr;  // 2 * sx * sz words
+    uint16_t* d_slabs = nullptr;  // words (+ 8 words of zero padding)
+};
+
+}  // namespace rle
+
+struct rle_scene {
+    int device = 0;
+    int nummaps = 0;
+    rle::Level lv[RLE_MAX_MIPS];
+    uint64_t device_bytes = 0;
+    uint64_t run_headers = 0;
+    uint64_t surface_voxels = 0;
+};
+
+namespace rle {
+
+// Host-side .rle4 parse + column-table build (no device work).
+struct HostLevel {
+    int sx = 0, sy = 0, sz = 0;
+    const uint16_t* slabs = nullptr;  // points into the caller's bytes
+    uint64_t words = 0;
+};
+rle_status parse_rle4(const void* bytes, size_t nbytes, HostLevel* levels, int* nummaps);
+rle_status build_table(const HostLevel& lv, uint32_t* table, uint64_t* run_headers,
+                       uint64_t* surface_voxels);
+
+// Kernel parameters of one ray map bound to one scene.  Everything the
+// device needs per frame, passed by value as a __grid_constant__.
+struct RayParams {
+    float p5x, p5y, p5z;          // p_2d[5] (z cleared as src/RayMap.h:206)
+    float p_no[8][3];
+    float to3d[4][4];
+    float p4[3];
+    float clip_min, clip_max;
+    int res[4];
+    float sin_x, cos_x, sin_y, cos_y, sin_ny, cos_ny;
+    float posx, posy, posz;
+    float rotx;
+    float focal;                  // (S/2) / fov_scale
+    int S;                        // samples per ray
+    int rays;                     // rays to cast
+    int mapswitch0;               // MIP_DISTANCE * (0.25*(4-|rot.x|)), src/Cuda_Render.h:335
+    int z_far;
+    int nummaps;
+    int gridx0, gridz0;
+    const uint2* table[RLE_MAX_MIPS];
+    const uint16_t* slabs[RLE_MAX_MIPS];
+    uint32_t* raybuf;
+    float* raydepth;
+    rle_hit* rayhit;
+    rle_counters* counters;
+};
+
+// Per-frame constants of the resolve (uniforms of colorize_buddha_soft.frag).
+struct ResolveParams {
+    float resx, resy;
+    float vanish_x, vanish_y;
+    float ofs_x, ofs_y, ofs_z, ofs_w;
+    float ratio;
+    float rxg0;
+    int width, height;
+    int S, rows;
+    int rays;                     // rows >= rays were not cast: no data
+    const uint32_t* raybuf;
+    const float* raydepth;
+    const rle_hit* rayhit;
+    uint32_t* colour;
+    float* depth;
+    rle_hit* hit;
+};
+
+rle_status fill_ray_params(const rle_scene* scene, const rle_raymap* rm, RayParams* p);
+rle_status fill_resolve_params(const rle_raymap* rm, ResolveParams* p);
+
+// Kernel launchers (render.cu, resolve.cu).
+rle_status launch_raycast(const RayParams& p, void* stream);
+rle_status launch_resolve(const ResolveParams& p, void* stream);
+
+}  // namespace rle

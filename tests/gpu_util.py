@@ -1,0 +1,66 @@
+"""Helpers for the GPU tests: device buffers and one-call renders through
+the C ABI, returned as host numpy arrays."""
+from __future__ import annotations
+
+import numpy as np
+
+
+class Frame:
+    """Ray buffer, depth, hits and counters of one ray map, plus the resolve."""
+
+    def __init__(self, torch, rle, scene, rm, hits: bool = True, counters: bool = True, stream: int = 0):
+        words = rle.raybuf_words(rm)
+        dev = "cuda"
+        self.raybuf = torch.empty(words, dtype=torch.int32, device=dev)
+        self.raydepth = torch.empty(words, dtype=torch.float32, device=dev)
+        self.rayhit = torch.empty(words * 8, dtype=torch.uint8, device=dev) if hits else None
+        self.counters = torch.zeros(6, dtype=torch.int64, device=dev) if counters else None
+        rle.render_rays(scene, rm, self.raybuf, self.raydepth, self.rayhit, self.counters, stream=stream)
+        self.rm = rm
+        self.torch = torch
+        self.rle = rle
+
+    def rays_host(self):
+        """(packed words, depth, hits, counters) of the cast rows only."""
+        self.torch.cuda.synchronize()
+        n = self.rm.rays * self.rm.samples
+        words = self.raybuf[:n].cpu().numpy().view(np.uint32)
+        depth = self.raydepth[:n].cpu().numpy()
+        hits = self.rayhit[: n * 8].cpu().numpy().view(self.rle.HIT_DTYPE) if self.rayhit is not None else None
+        cnt = self.counters.cpu().numpy() if self.counters is not None else None
+        return words, depth, hits, cnt
+
+    def resolve_host(self, hits: bool = True):
+        torch = self.torch
+        W, H = self.rm.width, self.rm.height
+        colour = torch.empty(W * H, dtype=torch.int32, device="cuda")
+        depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
+        hit = torch.empty(W * H * 8, dtype=torch.uint8, device="cuda") if hits else None
+        self.rle.resolve(self.rm, self.raybuf, self.raydepth, colour, depth, self.rayhit if hits else None, hit)
+        torch.cuda.synchronize()
+        return (colour.cpu().numpy().view(np.uint32), depth.cpu().numpy(),
+                hit.cpu().numpy().view(self.rle.HIT_DTYPE) if hit is not None else None)
+
+
+def counters_dict(arr) -> dict:
+    names = ("cells", "fetched", "headers", "runs", "spans", "pixels")
+    return {n: int(v) for n, v in zip(names, arr)}
+
+
+def oracle_counters(cnt) -> dict:
+    return {n: int(cnt[n].sum()) for n in cnt.dtype.names}
+
+
+def assert_rays_equal(gpu, orc, label=""):
+    """Packed words and hits bit-exact; depth bit-exact too (the stated bar
+    is 1e-5 relative, the implementation meets it with zero error)."""
+    gw, gd, gh, _ = gpu
+    ow, od, oh, _ = orc
+    assert gw.shape == ow.shape, label
+    bad = int((gw != ow).sum())
+    assert bad == 0, f"{label}: {bad} of {gw.size} ray-buffer words differ"
+    gbits, obits = gd.view(np.uint32), od.view(np.uint32)
+    dbad = int((gbits != obits).sum())
+    assert dbad == 0, f"{label}: {dbad} depths differ (max rel {np.nanmax(np.abs(gd - od) / np.abs(od)):.3g})"
+    if gh is not None and oh is not None:
+        assert np.array_equal(gh, oh), f"{label}: {int((gh != oh).sum())} hit records differ"

@@ -1,0 +1,167 @@
+"""Pins the CPU oracle to the reference.
+
+1. Against the golden fixtures (tests/golden/golden_v1.npz), which the
+   reference's own host build generated: column tables, ray maps and full ray
+   buffers must match bit for bit.  Runs everywhere.
+2. Against the reference's host build itself (oracle/_ref/libref.so), on
+   seeded random scenes and poses: encoder, mip rule, loader table, ray map
+   and per-ray raycast.  Runs where that library was built.
+"""
+from __future__ import annotations
+
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+
+def _golden_scene(po, golden):
+    levels = po.parse_rle4(golden["scene_rle4"].tobytes())
+    return levels, po.OracleScene(levels)
+
+
+def test_golden_tables(po, golden):
+    levels, _ = _golden_scene(po, golden)
+    for m, (sx, sy, sz, words) in enumerate(levels):
+        assert np.array_equal(po.build_table(words, sx, sz), golden[f"table_{m}"]), f"level {m}"
+
+
+def _golden_raymap(po, golden, i):
+    S, maxres, mipd, zfar = (int(v) for v in golden["params"])
+    border = float(golden["border"][0])
+    cam = golden[f"cam_{i}"]
+    rm = po.raymap_build(cam[:3], cam[3:], border, maxres, 1.0, S, mipd, zfar)
+    return rm
+
+
+@pytest.mark.parametrize("i", range(6))
+def test_golden_raymap(po, golden, i):
+    rm = _golden_raymap(po, golden, i)
+    f = po.ref_raymap_fields(golden[f"raymap_{i}"].tobytes())
+    bits = lambda a: np.asarray(a, np.float32).view(np.uint32)  # noqa: E731
+    assert list(rm.res) == list(f["res"])
+    assert rm.map_line_count == f["map_line_count"]
+    assert np.array_equal(bits([[v.x, v.y, v.z] for v in rm.p_2d]), bits(f["p_2d"]))
+    assert np.array_equal(bits([[v.x, v.y, v.z] for v in rm.p_no]), bits(f["p_no"]))
+    assert np.array_equal(bits(list(rm.to3d)), bits(f["to3d"]).ravel())
+    assert np.array_equal(bits(list(rm.p_ofs_min) + list(rm.p_ofs_max)),
+                          bits(np.concatenate([f["p_ofs_min"], f["p_ofs_max"]])))
+
+
+@pytest.mark.parametrize("i", range(6))
+def test_golden_raybuf(po, golden, i):
+    _, scene = _golden_scene(po, golden)
+    rm = _golden_raymap(po, golden, i)
+    out, depth, hits, cnt = po.render_rays(rm, scene, want_hits=True, want_counters=True)
+    ref = golden[f"raybuf_{i}"]
+    # the reference leaves samples outside a ray's clip range untouched (0 in
+    # a zeroed buffer); the oracle writes 0 there too
+    assert out.shape == ref.shape
+    assert np.array_equal(out, ref), f"{int((out != ref).sum())} of {out.size} samples differ"
+    hit = out != 0
+    assert ((hits["flags"] == 1) == (hit & (((out >> 16) & 0xFF) != 0xFF))).all()
+    assert cnt["pixels"].sum() == int((hits["flags"] == 1).sum())
+
+
+# ---------------------------------------------------------------------------
+# against the reference's host build (where it exists)
+# ---------------------------------------------------------------------------
+
+def _ref_built() -> bool:
+    from oracle import pyoracle
+    return pyoracle.ref_available()
+
+
+needs_ref = pytest.mark.skipif(not _ref_built(), reason="reference host build (oracle/_ref) not present")
+
+
+def _random_volume(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.arange(n)[None, :]
+    z = np.arange(n)[:, None]
+    h = n * 0.4 + n * 0.2 * np.sin(x * 2 * np.pi / n * 2 + seed) * np.cos(z * 2 * np.pi / n * 3) \
+        + rng.integers(0, 4, (n, n))
+    j = np.arange(n)[None, :, None]
+    vol = j >= (n - h[:, None, :])
+    cave = (rng.random((n // 4, n // 4, n // 4)) < 0.15).repeat(4, 0).repeat(4, 1).repeat(4, 2)
+    return vol & ~(cave & (j < n - 2))
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_encoder_and_mips_match_reference(po, seed):
+    n = 64
+    bits = po.pack_bits(_random_volume(n, seed))
+    for m in range(3):
+        s_ref, w_ref = po.ref_compress(bits, n, n, n, m)
+        s_orc, w_orc = po.encode_mip(bits, n, n, n, m)
+        assert np.array_equal(s_ref, s_orc) and np.array_equal(w_ref, w_orc)
+        nb_ref = po.ref_mipmap(bits, n, n, n)
+        nb_orc = po.mipmap(bits, n, n, n)
+        assert np.array_equal(nb_ref, nb_orc)
+        bits, n = nb_orc, n // 2
+
+
+@needs_ref
+def test_long_runs_split_like_reference(po):
+    """skip > 1023 and solid > 63 header splitting (src/Rle4.cpp:168-179)."""
+    sx, sy, sz = 8, 2048, 8
+    vol = np.zeros((sz, sy, sx), bool)
+    vol[:, 1500:, :] = True           # skip of 1500 then a thick solid block
+    vol[:, 200:330, 3] = True         # 130-voxel column-wide run
+    vol[2, :, :] = True               # a full-height wall (all surface at the edge)
+    bits = po.pack_bits(vol)
+    s_ref, w_ref = po.ref_compress(bits, sx, sy, sz, 0)
+    s_orc, w_orc = po.encode_mip(bits, sx, sy, sz, 0)
+    assert np.array_equal(w_ref, w_orc) and np.array_equal(s_ref, s_orc)
+    assert (w_orc == 1023).any() and ((w_orc >> 10) == 63).any()
+
+
+@needs_ref
+def test_loader_table_matches_reference(po):
+    n = 32
+    vol = _random_volume(n, 4)
+    vol[:, :, 7] = False  # empty columns exercise the read past the column (src/Rle4.cpp:301)
+    bits = [po.pack_bits(vol)]
+    dims = [(n, n, n)]
+    for _ in range(2):
+        bits.append(po.mipmap(bits[-1], *dims[-1]))
+        dims.append(tuple(d // 2 for d in dims[-1]))
+    levels = [(*dims[m], po.encode_mip(bits[m], *dims[m], m)[1]) for m in range(3)]
+    with tempfile.TemporaryDirectory() as td:
+        p = Path(td) / "t.rle4"
+        p.write_bytes(po.write_rle4(levels))
+        for m in range(3):
+            assert np.array_equal(po.ref_load_table(str(p), m, dims[m][0], dims[m][2]),
+                                  po.build_table(levels[m][3], dims[m][0], dims[m][2]))
+
+
+@needs_ref
+def test_raymap_and_raycast_match_reference(po):
+    n = 64
+    vol = _random_volume(n, 9)
+    bits = [po.pack_bits(vol)]
+    dims = [(n, n, n)]
+    for _ in range(3):
+        bits.append(po.mipmap(bits[-1], *dims[-1]))
+        dims.append(tuple(d // 2 for d in dims[-1]))
+    levels = [(*dims[m], po.encode_mip(bits[m], *dims[m], m)[1]) for m in range(4)]
+    scene = po.OracleScene(levels)
+    rng = np.random.default_rng(21)
+    S, maxres, border = 160, 160, 0.125
+    total = diff = 0
+    for _ in range(24):
+        pos = (float(rng.uniform(0, n)), float(-rng.uniform(10, 40)), float(rng.uniform(0, n)))
+        rot = (float(rng.choice([-1, 1]) * rng.uniform(0.05, 1.5)), float(rng.uniform(0, 6.3)), 0.0)
+        rb = po.ref_raymap(pos, rot, border, maxres)
+        f = po.ref_raymap_fields(rb)
+        rm = po.raymap_build(pos, rot, border, maxres, 1.0, S, 40, 1200)
+        assert list(rm.res) == list(f["res"])
+        assert np.array_equal(np.array(list(rm.to3d), np.float32).view(np.uint32), f["to3d"].ravel().view(np.uint32))
+        nr = po.rays_to_render(rm)
+        ref = po.ref_render_rays(rb, scene, S, nr, 40, 1200)
+        out, _, _, _ = po.render_rays(rm, scene)
+        total += out.size
+        diff += int((out != ref).sum())
+    assert diff == 0, f"{diff} of {total} samples differ"
