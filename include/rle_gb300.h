@@ -190,6 +190,19 @@ typedef struct rle_counters {
     unsigned long long pixels;   /* samples coloured (2 B colour read each) */
 } rle_counters;
 
+/* Launch shape of the raycast kernel (process-wide; 0 = built-in default).
+ *   lanes_per_ray      lanes of a warp cooperating on one column ray: 8, 16
+ *                      or 32 (4, 2 or 1 rays per warp); default 32
+ *   cells_per_lane     DDA steps each lane takes per chunk: 1 (reserved)
+ *   threads_per_block  32, 64, 96 or 128; default 128 */
+typedef struct rle_tuning {
+    int lanes_per_ray;
+    int cells_per_lane;
+    int threads_per_block;
+} rle_tuning;
+rle_status rle_tuning_set(const rle_tuning* t);
+rle_status rle_tuning_get(rle_tuning* t);
+
 /* Words of the ray buffer of a ray map: rows * samples. */
 size_t rle_raybuf_words(const rle_raymap* rm);
 

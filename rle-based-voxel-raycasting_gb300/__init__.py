@@ -9,4 +9,4 @@ from .api import *  # noqa: F401,F403
 from .api import (Camera, Counters, Hit, HIT_DTYPE, RayMap, RLEError, Scene, SceneInfo,  # noqa: F401
                   ScenegenParams, ViewParams, camera, ground_height, frame_workspace_bytes, library, ptr,
                   raybuf_words, raymap_build, render_frame, render_rays, resolve, scenegen_default,
-                  scenegen_dense, scenegen_rle4, version, view_params)
+                  scenegen_dense, scenegen_rle4, tuning_get, tuning_set, version, view_params)

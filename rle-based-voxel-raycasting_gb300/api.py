@@ -77,6 +77,13 @@ class Counters(C.Structure):
     _fields_ = [(n, C.c_ulonglong) for n in COUNTER_FIELDS]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("lanes_per_ray", C.c_int), ("cells_per_lane", C.c_int), ("threads_per_block", C.c_int)]
+
+
+RAYCAST_SHAPES = [(8, 1), (16, 1), (32, 1)]
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("device", C.c_int), ("nummaps", C.c_int), ("sx", C.c_int * RLE_MAX_MIPS),
                 ("sy", C.c_int * RLE_MAX_MIPS), ("sz", C.c_int * RLE_MAX_MIPS),
@@ -111,6 +118,8 @@ def _load() -> C.CDLL:
         "rle_host_free": (None, [vp]),
         "rle_raymap_build": (C.c_int, [C.POINTER(Camera), C.POINTER(ViewParams), C.POINTER(RayMap)]),
         "rle_raybuf_words": (C.c_size_t, [C.POINTER(RayMap)]),
+        "rle_tuning_set": (C.c_int, [C.POINTER(Tuning)]),
+        "rle_tuning_get": (C.c_int, [C.POINTER(Tuning)]),
         "rle_render_rays": (C.c_int, [vp, C.POINTER(RayMap), vp, vp, vp, vp, vp]),
         "rle_resolve": (C.c_int, [C.POINTER(RayMap), vp, vp, vp, vp, vp, vp, vp]),
         "rle_frame_workspace_bytes": (C.c_size_t, [C.POINTER(ViewParams)]),
@@ -271,6 +280,18 @@ def raymap_build(cam: Camera, view: ViewParams) -> RayMap:
 
 def raybuf_words(rm: RayMap) -> int:
     return int(_lib.rle_raybuf_words(C.byref(rm)))
+
+
+def tuning_set(lanes_per_ray: int = 0, cells_per_lane: int = 0, threads_per_block: int = 0) -> None:
+    """Process-wide launch shape of the raycast (0 = built-in default)."""
+    _check(_lib.rle_tuning_set(C.byref(Tuning(lanes_per_ray, cells_per_lane, threads_per_block))),
+           "rle_tuning_set")
+
+
+def tuning_get() -> tuple[int, int, int]:
+    t = Tuning()
+    _check(_lib.rle_tuning_get(C.byref(t)), "rle_tuning_get")
+    return t.lanes_per_ray, t.cells_per_lane, t.threads_per_block
 
 
 # ---------------------------------------------------------------------------

@@ -8,6 +8,7 @@
 // and nothing synchronises the host.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -120,6 +121,37 @@ struct DeviceGuard {
 }  // namespace
 }  // namespace rle
 
+namespace {
+std::atomic<int> g_lanes_per_ray{0};
+std::atomic<int> g_cells_per_lane{0};
+std::atomic<int> g_threads_per_block{0};
+
+bool shape_built(int lanes, int cells) {
+    return (lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32) && (cells == 0 || cells == 1);
+}
+}  // namespace
+
+extern "C" rle_status rle_tuning_set(const rle_tuning* t) {
+    if (!t) return RLE_ERR_INVALID_ARG;
+    const int l = t->lanes_per_ray, c = t->cells_per_lane, b = t->threads_per_block;
+    if (!shape_built(l, c) || b < 0 || b > 128 || b % 32 != 0) {
+        rle::set_error("rle_tuning_set: lanes_per_ray in {0,8,16,32}, cells_per_lane in {0,1}, threads_per_block in {0,32,..,128}");
+        return RLE_ERR_INVALID_ARG;
+    }
+    g_lanes_per_ray = l;
+    g_cells_per_lane = c;
+    g_threads_per_block = b;
+    return RLE_OK;
+}
+
+extern "C" rle_status rle_tuning_get(rle_tuning* t) {
+    if (!t) return RLE_ERR_INVALID_ARG;
+    t->lanes_per_ray = g_lanes_per_ray;
+    t->cells_per_lane = g_cells_per_lane;
+    t->threads_per_block = g_threads_per_block;
+    return RLE_OK;
+}
+
 extern "C" size_t rle_raybuf_words(const rle_raymap* rm) {
     if (!rm || rm->rows < 0 || rm->samples < 0) return 0;
     return static_cast<size_t>(rm->rows) * static_cast<size_t>(rm->samples);
@@ -139,6 +171,9 @@ extern "C" rle_status rle_render_rays(const rle_scene* scene, const rle_raymap* 
     p.raydepth = d_raydepth;
     p.rayhit = d_rayhit;
     p.counters = d_counters;
+    p.lanes_per_ray = g_lanes_per_ray;
+    p.cells_per_lane = g_cells_per_lane;
+    p.threads_per_block = g_threads_per_block;
     rle::DeviceGuard g(scene->device);
     if (!g.ok) {
         rle::set_error("rle_render_rays: cannot select device %d", scene->device);

@@ -1,24 +1,35 @@
 // Column-ray traversal on sm_103a.
 //
-// One thread casts one column ray through the 2D grid of RLE columns with
-// the reference's 2D DDA, picks the mip level by distance, walks each
-// visited column's run headers, projects solid runs to screen spans and
-// fills them with perspective-correct colour and depth, culling with a
-// floating horizon and a per-ray occupancy bitmask in shared memory
-// (Render::render_line, src/Cuda_Render.h:96-737, with the switches
-// FLOATING_HORIZON, XFLOATING_HORIZON and SHAREMEMCLIP of src/core.h:24-32).
+// Algorithm (Render::render_line, src/Cuda_Render.h:96-737, with the
+// switches FLOATING_HORIZON, XFLOATING_HORIZON and SHAREMEMCLIP of
+// src/core.h:24-32): a column ray marches the 2D grid of RLE columns with a
+// 2D DDA, picks the mip level by distance, walks each visited column's run
+// headers, projects solid runs to screen spans and fills them with
+// perspective-correct colour and depth, culling with a floating horizon and
+// an occupancy bitmask.
 //
-// Arithmetic: compiled with -fmad=false and IEEE division/square root, every
+// Parallel decomposition: a group of G lanes (G = 8, 16 or 32; 32/G rays
+// per warp) owns one ray.  The ray is processed in chunks of G DDA steps:
+//   1. lane k replays the DDA from the chunk start for k steps and takes
+//      step k (the DDA is a chain of IEEE additions, so every lane repeats
+//      the same operations); the last lane's state starts the next chunk;
+//   2. each lane, in parallel, derives its cell, pre-culls it against the
+//      horizon at the start of the chunk, fetches the column-table entry and
+//      scans the column's runs; a __ballot_sync gives the cells that may draw;
+//   3. the group walks those cells in order (values broadcast with
+//      __shfl_sync) and applies the exact sequential horizon logic; span
+//      pixels are interpolated and written by all G lanes at once.
+// The pre-cull is conservative: the horizon only closes (ymin grows, ymax
+// shrinks), so a cell or run culled at the chunk start would be culled at
+// its turn too.  The result is the sequential algorithm's, bit for bit.
+//
+// Arithmetic: compiled with -fmad=false and IEEE division/square root, each
 // float operation is the single IEEE operation the reference performs, in
-// its order, so results match the reference's host build bit for bit.  The
-// per-frame sines and cosines arrive precomputed from the host (the
-// reference evaluates the same host-side values per ray).
+// its order.  Per-frame sines/cosines come precomputed from the host.
 //
-// Output, per ray row (ray-major, `S` samples): every sample is written
-// exactly once -- coloured samples when they are drawn, the rest at the end
-// (sky 0x00ff8844 inside the ray's clip range, 0 outside).  The occupancy
-// bitmask (1 bit per sample) says which is which.  The reference instead
-// clears the clip range to sky first and never touches samples outside it.
+// Output, per ray row (ray-major, S samples): every sample is written once
+// -- coloured samples when drawn, the rest in a final coalesced pass (sky
+// 0x00ff8844 inside the ray's clip range, 0 outside), guided by the bitmask.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -33,28 +44,6 @@ constexpr uint32_t kSky = 0x00ff8844u;
 
 struct Counts {
     unsigned long long cells = 0, fetched = 0, headers = 0, runs = 0, spans = 0, pixels = 0;
-};
-
-// Occupancy bitmask of one ray: word w of thread t at smem[w * stride + t],
-// so lanes touching the same word index hit distinct banks.
-struct Mask {
-    uint32_t* base;
-    int stride;
-    __device__ __forceinline__ bool get(int y) const { return (base[(y >> 5) * stride] >> (y & 31)) & 1u; }
-    __device__ __forceinline__ void set(int y) const { base[(y >> 5) * stride] |= 1u << (y & 31); }
-    __device__ __forceinline__ uint32_t word(int w) const { return base[w * stride]; }
-    // first y in [y, end) whose bit is clear, or end
-    __device__ __forceinline__ int first_clear(int y, int end) const {
-        while (y < end) {
-            const uint32_t free_bits = ~word(y >> 5) >> (y & 31);
-            if (free_bits) {
-                const int r = y + (__ffs(free_bits) - 1);
-                return r < end ? r : end;
-            }
-            y = (y | 31) + 1;
-        }
-        return end;
-    }
 };
 
 struct F3 {
@@ -81,16 +70,48 @@ __device__ __forceinline__ F3 to3d(const RayParams& P, F3 v) {
               P.to3d[0][2] * v.x + P.to3d[1][2] * v.y + P.to3d[2][2] * v.z + P.to3d[3][2]);
 }
 
-// Casts ray x.  Writes coloured samples; returns the clip range through
-// ymin/ymax (ymax < ymin: the ray covers no samples).
-template <bool kHits, bool kCount>
-__device__ __forceinline__ void cast(const RayParams& P, int x, const Mask& mask, uint32_t* row, float* drow,
-                                     rle_hit* hrow, int& ymin_out, int& ymax_out, Counts& cnt) {
-    const int S = P.S;
-    const float res_x2 = static_cast<float>(S / 2);
-    const float res_y2 = res_x2;
+// First lane of the group a lane mask describes.
+__device__ __forceinline__ int lane_base(unsigned gmask) { return __ffs(gmask) - 1; }
 
-    // ---- 2D line of this ray in its fan, and its horizontal direction ----
+// Occupancy bitmask of one ray in shared memory (1 bit per sample).
+struct Mask {
+    uint32_t* w;
+    __device__ __forceinline__ bool get(int y) const { return (w[y >> 5] >> (y & 31)) & 1u; }
+    // first y in [y, end) whose bit is clear, or end
+    __device__ __forceinline__ int first_clear(int y, int end) const {
+        while (y < end) {
+            const uint32_t free_bits = ~w[y >> 5] >> (y & 31);
+            if (free_bits) {
+                const int r = y + (__ffs(free_bits) - 1);
+                return r < end ? r : end;
+            }
+            y = (y | 31) + 1;
+        }
+        return end;
+    }
+};
+
+// Per-ray constants after set-up.
+struct Ray {
+    float ray_x, ray_z;
+    float rmul;          // res_x2_mul_reverse (with the field-of-view focal length)
+    float pos3d_z_add, pos3d_y_add;
+    float fix_x, fix_y;
+    bool vertical;
+    int ymin, ymax;      // clip range at the start (ymax < ymin: the ray is empty)
+};
+
+// Ray set-up: fan, 2D line, 3D direction, sample range, DDA start
+// (src/Cuda_Render.h:129-304).  Returns false if the ray covers no samples.
+struct Dda {
+    float g0x, g0y, g1x, g1y, gd0, gd1;
+    float i0x, i0y, i1x, i1y, dd0, dd1;
+    float dd_now, pnx, pny;
+    int index;
+};
+
+__device__ __forceinline__ bool setup_ray(const RayParams& P, int x, Ray& R, Dda& D) {
+    const int S = P.S;
     const int r0 = P.res[0], r1 = P.res[1] + r0, r2 = P.res[2] + r1;
     int q = 0;
     if (x >= r2) q = 3;
@@ -127,17 +148,22 @@ __device__ __forceinline__ void cast(const RayParams& P, int x, const Mask& mask
         d.x = xx;
         d.z = zz;
     }
-    const float ray_x = d.x, ray_z = d.z;
-    const bool vertical = q < 2;
+    R.ray_x = d.x;
+    R.ray_z = d.z;
+    R.vertical = q < 2;
     const float sin_x = P.sin_x, cos_x = P.cos_x;
 
-    // ---- reverse texturing and the ray's sample range (:203-250) ----
     bool reverse = false;
-    if (vertical && ray_z <= 0) reverse = true;
-    if (!vertical && ray_x <= 0 && sin_x > 0) reverse = true;
-    if (!vertical && ray_x > 0 && sin_x < 0) reverse = true;
+    if (R.vertical && R.ray_z <= 0) reverse = true;
+    if (!R.vertical && R.ray_x <= 0 && sin_x > 0) reverse = true;
+    if (!R.vertical && R.ray_x > 0 && sin_x < 0) reverse = true;
     float rmul = reverse ? -P.focal : P.focal;
-    if (vertical) rmul = -rmul;
+    if (R.vertical) rmul = -rmul;
+    R.rmul = rmul;
+    R.pos3d_z_add = sin_x;
+    R.pos3d_y_add = (R.vertical ? cos_x : 0.0f) * rmul;
+    R.ymin = 0;
+    R.ymax = -1;
     const int p_add = reverse ? 1 : -2;
     int a1x = static_cast<int>(static_cast<float>(S) * p1.x) + p_add;
     int a1y = static_cast<int>(static_cast<float>(S) * p1.y) + p_add;
@@ -147,9 +173,9 @@ __device__ __forceinline__ void cast(const RayParams& P, int x, const Mask& mask
     a1y = min(max(a1y, 0), S - 1);
     a2x = min(max(a2x, 0), S - 1);
     a2y = min(max(a2y, 0), S - 1);
-    if (a1y == a2y) return;
-    int ymin = vertical ? S - 1 - a1y : S - 1 - a1x;
-    int ymax = vertical ? S - 1 - a2y : S - 1 - a2x;
+    if (a1y == a2y) return false;
+    int ymin = R.vertical ? S - 1 - a1y : S - 1 - a1x;
+    int ymax = R.vertical ? S - 1 - a2y : S - 1 - a2x;
     if (reverse) {
         ymin = S - 1 - ymin;
         ymax = S - 1 - ymax;
@@ -159,256 +185,513 @@ __device__ __forceinline__ void cast(const RayParams& P, int x, const Mask& mask
         ymin = ymax;
         ymax = t;
     }
-    if (ymin >= ymax) return;
-    ymin_out = ymin;
-    ymax_out = ymax;
+    if (ymin >= ymax) return false;
+    R.ymin = ymin;
+    R.ymax = ymax;
 
-    // ---- DDA set-up (:270-304) ----
-    const float dir_x = ray_x * P.cos_y + ray_z * P.sin_y;
-    const float dir_y = ray_x * P.sin_y - ray_z * P.cos_y;
-    float fix_x = -1, fix_y = -1, sign_x = -1, sign_y = -1;
+    const float dir_x = R.ray_x * P.cos_y + R.ray_z * P.sin_y;
+    const float dir_y = R.ray_x * P.sin_y - R.ray_z * P.cos_y;
+    float sign_x = -1, sign_y = -1;
+    R.fix_x = -1;
+    R.fix_y = -1;
     float frac_x = P.posx - static_cast<float>(static_cast<int>(P.posx));
     float frac_y = P.posz - static_cast<float>(static_cast<int>(P.posz));
-    if (dir_x >= 0) { fix_x = 0; sign_x = 1; frac_x = 1 - frac_x; }
-    if (dir_y >= 0) { fix_y = 0; sign_y = 1; frac_y = 1 - frac_y; }
-    float g0y = dir_y / fabsf(dir_x), g0x = sign_x;
-    float g1x = dir_x / fabsf(dir_y), g1y = sign_y;
-    float i0x = g0x * frac_x, i0y = g0y * frac_x;
-    float i1x = g1x * frac_y, i1y = g1y * frac_y;
-    float gd0 = sqrtf(g0x * g0x + g0y * g0y);
-    float gd1 = sqrtf(g1x * g1x + g1y * g1y);
-    float dd0 = sqrtf(i0x * i0x + i0y * i0y);
-    float dd1 = sqrtf(i1x * i1x + i1y * i1y);
-    float pbx = 0, pby = 0, dd_before = 0;
-    float pnx = 0, pny = 0, dd_now = 0;
-    int index = 0, index_before = 0;
+    if (dir_x >= 0) { R.fix_x = 0; sign_x = 1; frac_x = 1 - frac_x; }
+    if (dir_y >= 0) { R.fix_y = 0; sign_y = 1; frac_y = 1 - frac_y; }
+    D.g0y = dir_y / fabsf(dir_x);
+    D.g0x = sign_x;
+    D.g1x = dir_x / fabsf(dir_y);
+    D.g1y = sign_y;
+    D.i0x = D.g0x * frac_x;
+    D.i0y = D.g0y * frac_x;
+    D.i1x = D.g1x * frac_y;
+    D.i1y = D.g1y * frac_y;
+    D.gd0 = sqrtf(D.g0x * D.g0x + D.g0y * D.g0y);
+    D.gd1 = sqrtf(D.g1x * D.g1x + D.g1y * D.g1y);
+    D.dd0 = sqrtf(D.i0x * D.i0x + D.i0y * D.i0y);
+    D.dd1 = sqrtf(D.i1x * D.i1x + D.i1y * D.i1y);
+    D.dd_now = 0;
+    D.pnx = 0;
+    D.pny = 0;
+    D.index = 0;
+    return true;
+}
 
-    int mip = 0;
-    int gridx = P.gridx0, gridz = P.gridz0;
-    const uint2* table = P.table[0];
-    const uint16_t* slab_base = P.slabs[0];
-    const float pos3d_z_add = sin_x;
-    const float pos3d_y_add = (vertical ? cos_x : 0.0f) * rmul;
-    const float mountain = P.posy;
-    float z = 0, dz = 1;
-    float y_map_switch = P.posy;
-    int mapswitch = P.mapswitch0;
-    const float zfar = static_cast<float>(P.z_far);
+// One DDA cell as the merge needs it.
+struct Cell {
+    float pz, py, czz, cyy;
+    uint32_t ex, ey;  // column-table entry
+    int mip;
+    int vx, vz;
+    bool loaded;
+};
 
-    for (;;) {
-        while (z > static_cast<float>(mapswitch) || y_map_switch > 512.0f) {
-            y_map_switch = y_map_switch * 0.5f;
-            if (mip < P.nummaps - 1) {
-                mip++;
-                gridx >>= 1;
-                gridz >>= 1;
-                table = P.table[mip];
-                slab_base = P.slabs[mip];
-            }
-            g0x *= 2; g0y *= 2; g1x *= 2; g1y *= 2;
-            gd0 *= 2; gd1 *= 2;
-            mapswitch *= 2;
-            dz *= 2;
+template <int G>
+__device__ __forceinline__ void draw_run(const RayParams& P, const Ray& R, const Mask& mask, unsigned gmask,
+                                         int k, uint32_t* row, float* drow, rle_hit* hrow, const uint16_t* colours,
+                                         int y, int scr_y2, float sgs, float sgf, float tex, int texture,
+                                         float pz, float py, int mip, int vx, int vz, Counts& cnt, bool count) {
+    const float res_y2 = static_cast<float>(P.S / 2);
+    const float pz1r = pz + R.pos3d_z_add * sgs;
+    const float py1r = py + R.pos3d_y_add * sgs;
+    const float pz2r = pz + R.pos3d_z_add * sgf;
+    const float py2r = py + R.pos3d_y_add * sgf;
+    const float scr_y2r = res_y2 + py1r / pz1r;
+    const float scr_y1r = res_y2 + py2r / pz2r;
+    const float u1z = tex / pz2r;
+    float u2dz = static_cast<float>(texture) / pz1r - u1z;
+    const float onez1 = 1 / pz2r;
+    float onedz2 = 1 / pz1r - onez1;
+    u2dz /= scr_y2r - scr_y1r;
+    onedz2 /= scr_y2r - scr_y1r;
+    if (count) cnt.spans++;
+    const float mult = static_cast<float>(y + 1) - scr_y1r;
+    float uz = u1z + u2dz * mult;
+    float onez = onez1 + onedz2 * mult;
+    const float umin = static_cast<float>(texture);
+    const float umax = static_cast<float>(static_cast<double>(tex) - 1.0);
+    // G pixels per pass: the accumulation runs in lockstep in every lane (it
+    // is a chain of IEEE additions, one per sample, masked or not); lane k
+    // keeps the values of sample y + k and does its divisions in parallel.
+    for (int y0 = y; y0 < scr_y2; y0 += G) {
+        const int n = min(G, scr_y2 - y0);
+        // lane k needs the accumulators after k more additions
+        float my_uz = uz, my_onez = onez;
+        for (int j = 0; j < k && j < n; j++) {
+            my_uz += u2dz;
+            my_onez += onedz2;
         }
-        z += dz;
-        if (z > zfar) return;
-        if (ymin >= ymax) return;
-
-        dd_before = dd_now;
-        pbx = pnx;
-        pby = pny;
-        index_before = index;
-        if (dd1 < dd0) {
-            dd_now = dd1;
-            index = 1;
-            dd1 += gd1;
-            pnx = i1x; pny = i1y;
-            i1x += g1x;
-            i1y += g1y;
-        } else {
-            dd_now = dd0;
-            index = 0;
-            pnx = i0x; pny = i0y;
-            dd0 += gd0;
-            i0x += g0x;
-            i0y += g0y;
+        if (n == G) {  // start of the next pass: G additions from this one
+            uz = __shfl_sync(gmask, my_uz, (lane_base(gmask)) + G - 1) + u2dz;
+            onez = __shfl_sync(gmask, my_onez, (lane_base(gmask)) + G - 1) + onedz2;
         }
-        if (kCount) cnt.cells++;
-        const int fxi = static_cast<int>(static_cast<float>(1 - index_before) * fix_x);
-        const int fzi = static_cast<int>(static_cast<float>(index_before) * fix_y);
-        const float dd_delta = dd_now - dd_before;
-        const float vs_x = ray_x * dd_before;
-        const float vs_z = ray_z * dd_before;
-        const int voxel_x = static_cast<int>(P.posx + pbx) + fxi;
-        const int voxel_z = static_cast<int>(P.posz + pby) + fzi;
-        const int vx = (voxel_x >> mip) & (gridx - 1);
-        const int vz = (voxel_z >> mip) & (gridz - 1);
-        const float corr_x = ray_x * dd_delta;
-        const float corr_z = ray_z * dd_delta;
-        const float pz = cos_x * vs_z + sin_x * mountain;
-        float py = vertical ? cos_x * mountain - sin_x * vs_z : vs_x;
-        py *= rmul;
-
-        // clip top (:467)
-        if (pz * res_y2 + py <= pz * static_cast<float>(ymin)) continue;
-
-        const uint2 entry = __ldg(&table[static_cast<size_t>(vx) + static_cast<size_t>(vz) * gridx]);
-        if (kCount) cnt.fetched++;
-        const float czz = cos_x * corr_z;
-        float cyy = vertical ? -sin_x * corr_z : corr_x;
-        cyy *= rmul;
-
-        const uint16_t* hdr = slab_base + 2 + entry.x;
-        const int nruns = entry.y & 0xffffu;
-        const uint16_t* colours = hdr + nruns;
-        uint32_t sti = entry.y >> 16;
-        int sg = 0;       // sti_general: height below the next run, level-0 units
-        float tex = 0;    // colour index of the next run's first voxel
-
-        for (int r = 0; r < nruns; r++) {
-            if (r > 0) {
-                sti = __ldg(&hdr[r]);
-                if (kCount) cnt.headers++;
+        const int yy = y0 + k;
+        bool wrote = false;
+        if (yy < scr_y2 && !mask.get(yy)) {
+            const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(my_uz / my_onez, umin), umax));
+            const float depth = 1 / my_onez;
+            const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
+            const uint32_t c16 = __ldg(&colours[u]);
+            row[yy] = c16 + (real_z << 16);
+            drow[yy] = depth;
+            if (hrow) {
+                rle_hit h;
+                h.x = static_cast<uint16_t>(vx);
+                h.z = static_cast<uint16_t>(vz);
+                h.y = static_cast<uint16_t>((static_cast<int>(sgs) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
+                h.mip = static_cast<uint8_t>(mip);
+                h.flags = 1;
+                hrow[yy] = h;
             }
-            int solid = static_cast<int>(sti >> 10);
-            sg += static_cast<int>(sti & 1023u) << mip;
-            if (solid == 0) continue;
-            const int texture = static_cast<int>(tex);
-            tex += static_cast<float>(solid);
-            solid <<= mip;
-            const float sgs = static_cast<float>(sg);  // run bottom
-            sg += solid;
-            const float sgf = static_cast<float>(sg);  // run top
-            if (kCount) cnt.runs++;
-
-            float czz1 = pz, cyy1 = py;
-            if (mountain + sgs >= 0) { czz1 += czz; cyy1 += cyy; }
-            const float pz1 = czz1 + pos3d_z_add * sgs;
-            if (pz1 <= 0) continue;
-            const float py1 = cyy1 + pos3d_y_add * sgs;
-            int scr_y2 = static_cast<int>(res_y2 + py1 / pz1);
-            if (scr_y2 <= ymin) break;
-
-            float czz2 = pz, cyy2 = py;
-            if (mountain + sgf < 0) { czz2 += czz; cyy2 += cyy; }
-            const float pz2 = czz2 + pos3d_z_add * sgf;
-            if (pz2 <= 0) continue;
-            const float py2 = cyy2 + pos3d_y_add * sgf;
-            int scr_y1 = static_cast<int>(res_y2 + py2 / pz2 - 1);
-            if (scr_y1 >= ymax) continue;
-
-            // floating horizon (:563-580)
-            if (scr_y2 >= ymax) {
-                scr_y2 = ymax;
-                ymax = scr_y1;
-            }
-            if (scr_y1 <= ymin) {
-                scr_y1 = ymin;
-                ymin = scr_y2;
-                ymin = mask.first_clear(ymin, ymax > ymin ? ymax : ymin);
-            }
-            int y = mask.first_clear(scr_y1, scr_y2);
-            if (y >= scr_y2) continue;
-
-            // perspective-correct interpolation (:645-680)
-            const float pz1r = pz + pos3d_z_add * sgs;
-            const float py1r = py + pos3d_y_add * sgs;
-            const float pz2r = pz + pos3d_z_add * sgf;
-            const float py2r = py + pos3d_y_add * sgf;
-            const float scr_y2r = res_y2 + py1r / pz1r;
-            const float scr_y1r = res_y2 + py2r / pz2r;
-            const float u1z = tex / pz2r;
-            float u2dz = static_cast<float>(texture) / pz1r - u1z;
-            const float onez1 = 1 / pz2r;
-            float onedz2 = 1 / pz1r - onez1;
-            u2dz /= scr_y2r - scr_y1r;
-            onedz2 /= scr_y2r - scr_y1r;
-            if (kCount) cnt.spans++;
-            const float mult = static_cast<float>(y + 1) - scr_y1r;
-            float uz = u1z + u2dz * mult;
-            float onez = onez1 + onedz2 * mult;
-            const float umin = static_cast<float>(texture);
-            const float umax = static_cast<float>(static_cast<double>(tex) - 1.0);
-            for (; y < scr_y2; ++y, uz += u2dz, onez += onedz2) {
-                if (mask.get(y)) continue;
-                const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(uz / onez, umin), umax));
-                const float depth = 1 / onez;
-                const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
-                const uint32_t c16 = __ldg(&colours[u]);
-                row[y] = c16 + (real_z << 16);
-                drow[y] = depth;
-                if (kHits) {
-                    rle_hit h;
-                    h.x = static_cast<uint16_t>(vx);
-                    h.z = static_cast<uint16_t>(vz);
-                    h.y = static_cast<uint16_t>((static_cast<int>(sgs) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
-                    h.mip = static_cast<uint8_t>(mip);
-                    h.flags = 1;
-                    hrow[y] = h;
-                }
-                if (kCount) cnt.pixels++;
-                mask.set(y);
-            }
+            atomicOr(&mask.w[yy >> 5], 1u << (yy & 31));
+            wrote = true;
         }
+        if (count) cnt.pixels += __popc(__ballot_sync(gmask, wrote));
+        __syncwarp(gmask);
     }
 }
 
-template <bool kHits, bool kCount>
-__global__ void raycast_kernel(const __grid_constant__ RayParams P) {
+// Exact sequential processing of one cell (the body of the reference's main
+// loop after the DDA step).  Uniform across the G lanes of the group.
+template <int G>
+__device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, const Mask& mask, unsigned gmask, int k,
+                                           uint32_t* row, float* drow, rle_hit* hrow, Cell c, int& ymin, int& ymax,
+                                           Counts& cnt, bool count) {
+    const float res_y2 = static_cast<float>(P.S / 2);
+    // clip top (:467)
+    if (c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin)) return;
+    if (!c.loaded) {
+        const uint2 e = __ldg(&P.table[c.mip][static_cast<size_t>(c.vx) +
+                                              static_cast<size_t>(c.vz) * (P.gridx0 >> c.mip)]);
+        c.ex = e.x;
+        c.ey = e.y;
+    }
+    if (count) cnt.fetched++;
+    const uint16_t* hdr = P.slabs[c.mip] + 2 + c.ex;
+    const int nruns = c.ey & 0xffffu;
+    const uint16_t* colours = hdr + nruns;
+    const float mountain = P.posy;
+    uint32_t sti = c.ey >> 16;
+    int sg = 0;
+    float tex = 0;
+    for (int r = 0; r < nruns; r++) {
+        if (r > 0) {
+            sti = __ldg(&hdr[r]);
+            if (count) cnt.headers++;
+        }
+        int solid = static_cast<int>(sti >> 10);
+        sg += static_cast<int>(sti & 1023u) << c.mip;
+        if (solid == 0) continue;
+        const int texture = static_cast<int>(tex);
+        tex += static_cast<float>(solid);
+        solid <<= c.mip;
+        const float sgs = static_cast<float>(sg);
+        sg += solid;
+        const float sgf = static_cast<float>(sg);
+        if (count) cnt.runs++;
+        float czz1 = c.pz, cyy1 = c.py;
+        if (mountain + sgs >= 0) { czz1 += c.czz; cyy1 += c.cyy; }
+        const float pz1 = czz1 + R.pos3d_z_add * sgs;
+        if (pz1 <= 0) continue;
+        const float py1 = cyy1 + R.pos3d_y_add * sgs;
+        int scr_y2 = static_cast<int>(res_y2 + py1 / pz1);
+        if (scr_y2 <= ymin) break;
+        float czz2 = c.pz, cyy2 = c.py;
+        if (mountain + sgf < 0) { czz2 += c.czz; cyy2 += c.cyy; }
+        const float pz2 = czz2 + R.pos3d_z_add * sgf;
+        if (pz2 <= 0) continue;
+        const float py2 = cyy2 + R.pos3d_y_add * sgf;
+        int scr_y1 = static_cast<int>(res_y2 + py2 / pz2 - 1);
+        if (scr_y1 >= ymax) continue;
+        // floating horizon (:563-580)
+        if (scr_y2 >= ymax) {
+            scr_y2 = ymax;
+            ymax = scr_y1;
+        }
+        if (scr_y1 <= ymin) {
+            scr_y1 = ymin;
+            ymin = scr_y2;
+            ymin = mask.first_clear(ymin, ymax > ymin ? ymax : ymin);
+        }
+        const int y = mask.first_clear(scr_y1, scr_y2);
+        if (y >= scr_y2) continue;
+        draw_run<G>(P, R, mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sgs, sgf, tex, texture,
+                           c.pz, c.py, c.mip, c.vx, c.vz, cnt, count);
+    }
+}
+
+
+// Where the DDA of one ray stands between chunks (uniform in its group).
+struct Walk {
+    Dda d;
+    float z, dz, zswitch;
+    int mapswitch, mip;
+};
+
+// One DDA step (:376-414).  Uniform groups (G == 32: one ray per warp) take
+// the branch; smaller groups use selects so rays sharing a warp do not diverge.
+template <bool kBranch>
+__device__ __forceinline__ void dda_step(Dda& d) {
+    if (kBranch) {
+        if (d.dd1 < d.dd0) {
+            d.dd_now = d.dd1;
+            d.index = 1;
+            d.dd1 += d.gd1;
+            d.pnx = d.i1x;
+            d.pny = d.i1y;
+            d.i1x += d.g1x;
+            d.i1y += d.g1y;
+        } else {
+            d.dd_now = d.dd0;
+            d.index = 0;
+            d.pnx = d.i0x;
+            d.pny = d.i0y;
+            d.dd0 += d.gd0;
+            d.i0x += d.g0x;
+            d.i0y += d.g0y;
+        }
+    } else {
+        const bool c1 = d.dd1 < d.dd0;
+        d.dd_now = c1 ? d.dd1 : d.dd0;
+        d.index = c1 ? 1 : 0;
+        d.pnx = c1 ? d.i1x : d.i0x;
+        d.pny = c1 ? d.i1y : d.i0y;
+        const float n1 = d.dd1 + d.gd1, n0 = d.dd0 + d.gd0;
+        const float a1x = d.i1x + d.g1x, a1y = d.i1y + d.g1y;
+        const float a0x = d.i0x + d.g0x, a0y = d.i0y + d.g0y;
+        d.dd1 = c1 ? n1 : d.dd1;
+        d.i1x = c1 ? a1x : d.i1x;
+        d.i1y = c1 ? a1y : d.i1y;
+        d.dd0 = c1 ? d.dd0 : n0;
+        d.i0x = c1 ? d.i0x : a0x;
+        d.i0y = c1 ? d.i0y : a0y;
+    }
+}
+
+// Level-of-detail switch at the top of a step (:343-365): past the switch
+// distance the ray moves to the next mip level and doubles its step.
+__device__ __forceinline__ void lod_switch(Walk& w, int nummaps) {
+    while (w.z > w.zswitch) {
+        if (w.mip < nummaps - 1) w.mip++;
+        w.d.g0x *= 2; w.d.g0y *= 2; w.d.g1x *= 2; w.d.g1y *= 2;
+        w.d.gd0 *= 2; w.d.gd1 *= 2;
+        w.mapswitch *= 2;
+        w.zswitch = static_cast<float>(w.mapswitch);
+        w.dz *= 2;
+    }
+}
+
+// Derives the cell of one DDA step, pre-culls it against the horizon at the
+// start of the chunk, fetches its column-table entry and scans its runs.
+// Returns whether the exact walk could draw from it.
+__device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, bool valid, float before, float delta,
+                                             float pbx, float pby, int ib, int mip, int ymin, int ymax, Cell& c) {
+    const float res_y2 = static_cast<float>(P.S / 2);
+    const float sin_x = P.sin_x, cos_x = P.cos_x;
+    const float mountain = P.posy;
+    const int fxi = ib ? 0 : static_cast<int>(R.fix_x);
+    const int fzi = ib ? static_cast<int>(R.fix_y) : 0;
+    const float vs_x = R.ray_x * before;
+    const float vs_z = R.ray_z * before;
+    const int voxel_x = static_cast<int>(P.posx + pbx) + fxi;
+    const int voxel_z = static_cast<int>(P.posz + pby) + fzi;
+    c.mip = mip;
+    c.vx = (voxel_x >> mip) & ((P.gridx0 >> mip) - 1);
+    c.vz = (voxel_z >> mip) & ((P.gridz0 >> mip) - 1);
+    const float corr_x = R.ray_x * delta;
+    const float corr_z = R.ray_z * delta;
+    c.pz = cos_x * vs_z + sin_x * mountain;
+    const float py = R.vertical ? cos_x * mountain - sin_x * vs_z : vs_x;
+    c.py = py * R.rmul;
+    c.czz = cos_x * corr_z;
+    const float cyy = R.vertical ? -sin_x * corr_z : corr_x;
+    c.cyy = cyy * R.rmul;
+    c.ex = 0;
+    c.ey = 0;
+    // clip top at the chunk's horizon; for pz >= 0 it only gets truer as ymin grows
+    const bool culled = c.pz >= 0.0f && c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin);
+    c.loaded = valid && !culled;
+    if (!c.loaded) return false;
+    const uint2 e = __ldg(&P.table[mip][static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip)]);
+    c.ex = e.x;
+    c.ey = e.y;
+    // any run that could still draw at the chunk's horizon?  (runs culled
+    // here are culled by the exact walk too: ymin only grows, ymax only shrinks)
+    const uint16_t* hdr = P.slabs[mip] + 2 + c.ex;
+    const int nruns = c.ey & 0xffffu;
+    uint32_t sti = c.ey >> 16;
+    int sg = 0;
+    for (int r = 0; r < nruns; r++) {
+        if (r > 0) sti = __ldg(&hdr[r]);
+        int solid = static_cast<int>(sti >> 10);
+        sg += static_cast<int>(sti & 1023u) << mip;
+        if (solid == 0) continue;
+        solid <<= mip;
+        const float sgs = static_cast<float>(sg);
+        sg += solid;
+        const float sgf = static_cast<float>(sg);
+        float czz1 = c.pz, cyy1 = c.py;
+        if (mountain + sgs >= 0) { czz1 += c.czz; cyy1 += c.cyy; }
+        const float pz1 = czz1 + R.pos3d_z_add * sgs;
+        if (pz1 <= 0) continue;
+        const float py1 = cyy1 + R.pos3d_y_add * sgs;
+        const int scr_y2 = static_cast<int>(res_y2 + py1 / pz1);
+        if (scr_y2 <= ymin) return false;
+        float czz2 = c.pz, cyy2 = c.py;
+        if (mountain + sgf < 0) { czz2 += c.czz; cyy2 += c.cyy; }
+        const float pz2 = czz2 + R.pos3d_z_add * sgf;
+        if (pz2 <= 0) continue;
+        const float py2 = cyy2 + R.pos3d_y_add * sgf;
+        const int scr_y1 = static_cast<int>(res_y2 + py2 / pz2 - 1);
+        if (scr_y1 >= ymax) continue;
+        return true;
+    }
+    return false;
+}
+
+// G lanes per ray; chunks of G DDA steps, lane k taking step k of each.
+template <int G>
+__global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ RayParams P) {
+    constexpr int kGroups = 32 / G;
     extern __shared__ uint32_t smem[];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int g = lane / G;   // ray group within the warp
+    const int k = lane % G;   // lane within the group
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (g * G));
+    const int warp_in_block = threadIdx.x >> 5;
+    const int rays_per_block = (blockDim.x >> 5) * kGroups;
+    const int slot = warp_in_block * kGroups + g;  // ray slot within the block
+    const int x = blockIdx.x * rays_per_block + slot;
+    const int S = P.S;
+    const int words = (S + 31) >> 5;
+    const bool hits = P.rayhit != nullptr;
+    const bool count = P.counters != nullptr;
+    Mask mask{smem + slot * words};
     Counts cnt;
-    if (x < P.rays) {
-        const int S = P.S;
-        const int words = (S + 31) >> 5;
-        const Mask mask{smem + threadIdx.x, static_cast<int>(blockDim.x)};
-        for (int w = 0; w < words; w++) mask.base[w * mask.stride] = 0;
-        uint32_t* row = P.raybuf + static_cast<size_t>(x) * S;
-        float* drow = P.raydepth + static_cast<size_t>(x) * S;
-        rle_hit* hrow = kHits ? P.rayhit + static_cast<size_t>(x) * S : nullptr;
-        int ymin = 0, ymax = -1;
-        cast<kHits, kCount>(P, x, mask, row, drow, hrow, ymin, ymax, cnt);
-        // every sample not coloured: sky inside the clip range, none outside
-        for (int y = 0; y < S; y++) {
+    const bool active = x < P.rays;
+
+    Ray R;
+    Walk W;
+    bool live = false;
+    if (active) {
+        for (int w = k; w < words; w += G) mask.w[w] = 0;
+        live = setup_ray(P, x, R, W.d);
+    } else {
+        R.ymin = 0;
+        R.ymax = -1;
+    }
+    __syncwarp();
+    uint32_t* row = active ? P.raybuf + static_cast<size_t>(x) * S : nullptr;
+    float* drow = active ? P.raydepth + static_cast<size_t>(x) * S : nullptr;
+    rle_hit* hrow = (hits && active) ? P.rayhit + static_cast<size_t>(x) * S : nullptr;
+    const int ymin0 = R.ymin, ymax0 = R.ymax;
+
+    if (live) {
+        const float zfar = static_cast<float>(P.z_far);
+        int ymin = R.ymin, ymax = R.ymax;
+        W.mip = 0;
+        W.z = 0;
+        W.dz = 1;
+        W.mapswitch = P.mapswitch0;
+        W.zswitch = static_cast<float>(W.mapswitch);
+        {
+            // first step's switch test, the only one the camera height can
+            // trigger: y_map_switch starts at position.y and only halves
+            float y_map_switch = P.posy;
+            while (W.z > W.zswitch || y_map_switch > 512.0f) {
+                y_map_switch = y_map_switch * 0.5f;
+                if (W.mip < P.nummaps - 1) W.mip++;
+                W.d.g0x *= 2; W.d.g0y *= 2; W.d.g1x *= 2; W.d.g1y *= 2;
+                W.d.gd0 *= 2; W.d.gd1 *= 2;
+                W.mapswitch *= 2;
+                W.zswitch = static_cast<float>(W.mapswitch);
+                W.dz *= 2;
+            }
+        }
+        for (;;) {
+            // ---- 1. G DDA steps in lockstep; lane k keeps the state after step k ----
+            // the state before step k is the state after step k-1 (a shuffle
+            // from lane k-1; lane 0 takes the chunk start)
+            const float start_dd = W.d.dd_now, start_px = W.d.pnx, start_py = W.d.pny;
+            const int start_ix = W.d.index;
+            float c_dd = 0, c_px = 0, c_py = 0;
+            int c_ix = 0, smip = W.mip;
+            int nvalid = G;
+            // z, dz and the switch distances are integers held exactly in
+            // floats: when neither a LOD switch nor the end of the ray can
+            // fall inside the chunk, the steps need no checks
+            const int zi = static_cast<int>(W.z), dzi = static_cast<int>(W.dz);
+            const bool plain = W.mapswitch >= zi && (W.mapswitch - zi) / dzi + 1 >= G && (P.z_far - zi) / dzi >= G;
+            if (plain) {
+#pragma unroll
+                for (int s = 0; s < G; s++) {
+                    dda_step<G == 32>(W.d);
+                    if (s == k) {
+                        c_dd = W.d.dd_now;
+                        c_px = W.d.pnx;
+                        c_py = W.d.pny;
+                        c_ix = W.d.index;
+                    }
+                }
+                W.z += W.dz * static_cast<float>(G);
+            } else {
+                bool ended_here = false;
+#pragma unroll 1
+                for (int s = 0; s < G; s++) {
+                    if (W.z > W.zswitch) {
+                        lod_switch(W, P.nummaps);
+                        if (k >= s) smip = W.mip;  // cells from step s on use the new level
+                    }
+                    W.z += W.dz;
+                    if (W.z > zfar) {
+                        nvalid = s;
+                        ended_here = true;
+                        break;
+                    }
+                    dda_step<G == 32>(W.d);
+                    if (s == k) {
+                        c_dd = W.d.dd_now;
+                        c_px = W.d.pnx;
+                        c_py = W.d.pny;
+                        c_ix = W.d.index;
+                    }
+                }
+                (void)ended_here;
+            }
+            if (nvalid == 0) break;
+            const bool ended = nvalid < G;
+            const bool valid = k < nvalid;
+            float before = __shfl_up_sync(gmask, c_dd, 1);
+            float pbx = __shfl_up_sync(gmask, c_px, 1);
+            float pby = __shfl_up_sync(gmask, c_py, 1);
+            int ib = __shfl_up_sync(gmask, c_ix, 1);
+            if (k == 0) {
+                before = start_dd;
+                pbx = start_px;
+                pby = start_py;
+                ib = start_ix;
+            }
+            const float delta = c_dd - before;
+
+            // ---- 2. each lane: its cell -- pre-cull, fetch, run scan ----
+            Cell c;
+            const bool drawable = prepare_cell(P, R, valid, before, delta, pbx, pby, ib, smip, ymin, ymax, c);
+            // with counters every valid cell goes through the exact walk
+            unsigned todo = __ballot_sync(gmask, count ? valid : drawable) >> lane_base(gmask);
+            if (G < 32) todo &= (1u << G) - 1u;
+
+            // ---- 3. exact sequential merge of the cells that may draw ----
+            bool stop = false;
+            while (todo) {
+                const int s = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int src = lane_base(gmask) + s;
+                Cell cs;
+                cs.pz = __shfl_sync(gmask, c.pz, src);
+                cs.py = __shfl_sync(gmask, c.py, src);
+                cs.czz = __shfl_sync(gmask, c.czz, src);
+                cs.cyy = __shfl_sync(gmask, c.cyy, src);
+                cs.ex = __shfl_sync(gmask, c.ex, src);
+                cs.ey = __shfl_sync(gmask, c.ey, src);
+                cs.mip = __shfl_sync(gmask, c.mip, src);
+                cs.vx = __shfl_sync(gmask, c.vx, src);
+                cs.vz = __shfl_sync(gmask, c.vz, src);
+                cs.loaded = __shfl_sync(gmask, static_cast<int>(c.loaded), src) != 0;
+                // the reference ends the ray when its horizon closes, checked
+                // at every step before the cell (:370)
+                if (ymin >= ymax) {
+                    stop = true;
+                    break;
+                }
+                if (count) cnt.cells++;  // with counters every valid step is visited
+                merge_cell<G>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, cnt, count);
+            }
+            if (stop || ymin >= ymax || ended) break;
+        }
+    }
+    __syncwarp();
+
+    // ---- coalesced fill of the samples no span coloured ----
+    if (active) {
+        for (int y = k; y < S; y += G) {
             if (mask.get(y)) continue;
-            const bool in = y >= ymin && y <= ymax;
+            const bool in = y >= ymin0 && y <= ymax0;
             row[y] = in ? kSky : 0u;
             drow[y] = in ? INFINITY : 0.0f;
-            if (kHits) {
+            if (hrow) {
                 rle_hit h = {0, 0, 0, 0, static_cast<uint8_t>(in ? 2 : 0)};
                 hrow[y] = h;
             }
         }
     }
-    if (kCount) {
+    if (count) {
         unsigned long long v[6] = {cnt.cells, cnt.fetched, cnt.headers, cnt.runs, cnt.spans, cnt.pixels};
         for (int i = 0; i < 6; i++) {
-            unsigned long long s = v[i];
+            // the lanes of a group hold the same counts: take lane 0's
+            unsigned long long s = (k == 0) ? v[i] : 0ull;
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if ((threadIdx.x & 31) == 0 && s) atomicAdd(&reinterpret_cast<unsigned long long*>(P.counters)[i], s);
+            if (lane == 0 && s) atomicAdd(&reinterpret_cast<unsigned long long*>(P.counters)[i], s);
         }
     }
 }
 
-template <bool kHits, bool kCount>
-rle_status launch_variant(const RayParams& p, cudaStream_t stream) {
+template <int G>
+rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
     const int words = (p.S + 31) >> 5;
-    // 128 threads per block while their bitmasks fit in 200 KB of shared memory
-    int threads = 128;
-    while (threads > 32 && static_cast<size_t>(threads) * words * 4 > 200 * 1024) threads -= 32;
-    const size_t smem = static_cast<size_t>(threads) * words * 4;
+    const int rays_per_block = threads / 32 * (32 / G);
+    const size_t smem = static_cast<size_t>(rays_per_block) * words * 4;
     if (smem > 227 * 1024) {
-        set_error("rle_render_rays: %d samples per ray exceed the shared-memory bitmask", p.S);
+        set_error("rle_render_rays: %d samples per ray exceed shared memory at this launch shape", p.S);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<kHits, kCount>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
     }
-    const int blocks = (p.rays + threads - 1) / threads;
-    raycast_kernel<kHits, kCount><<<blocks, threads, smem, stream>>>(p);
+    const int blocks = (p.rays + rays_per_block - 1) / rays_per_block;
+    raycast_kernel<G><<<blocks, threads, smem, stream>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("raycast launch: %s", cudaGetErrorString(e));
@@ -422,11 +705,20 @@ rle_status launch_variant(const RayParams& p, cudaStream_t stream) {
 rle_status launch_raycast(const RayParams& p, void* stream) {
     if (p.rays <= 0) return RLE_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const bool hits = p.rayhit != nullptr, count = p.counters != nullptr;
-    if (hits && count) return launch_variant<true, true>(p, s);
-    if (hits) return launch_variant<true, false>(p, s);
-    if (count) return launch_variant<false, true>(p, s);
-    return launch_variant<false, false>(p, s);
+    const int lanes = p.lanes_per_ray > 0 ? p.lanes_per_ray : 32;
+    const int threads = p.threads_per_block > 0 ? p.threads_per_block : 128;
+    if (threads % 32 != 0 || threads > 128) {
+        set_error("raycast: threads per block must be a multiple of 32, at most 128");
+        return RLE_ERR_INVALID_ARG;
+    }
+    switch (lanes) {
+        case 8: return launch_shape<8>(p, threads, s);
+        case 16: return launch_shape<16>(p, threads, s);
+        case 32: return launch_shape<32>(p, threads, s);
+        default:
+            set_error("raycast: lanes per ray must be 8, 16 or 32");
+            return RLE_ERR_INVALID_ARG;
+    }
 }
 
 }  // namespace rle

@@ -73,6 +73,11 @@ struct RayParams {
     float* raydepth;
     rle_hit* rayhit;
     rle_counters* counters;
+    // launch shape (0 = default): lanes cooperating on one ray, DDA steps
+    // each lane claims per chunk, block size
+    int lanes_per_ray;
+    int cells_per_lane;
+    int threads_per_block;
 };
 
 // Per-frame constants of the resolve (uniforms of colorize_buddha_soft.frag).
