@@ -237,6 +237,27 @@ rle_status rle_render_frame(const rle_scene* scene, const rle_camera* cam,
                             size_t workspace_bytes, uint32_t* d_colour, float* d_depth,
                             rle_hit* d_hit, void* stream);
 
+/* Camera to screen without any device allocation (no counterpart in the
+ * reference).  For callers that may not allocate device memory while they
+ * run -- a render loop with a hard frame budget (cudaMalloc can synchronise
+ * the device), or a plug-in whose host application owns the GPU memory
+ * budget.  Same result as rle_render_frame without hit records.
+ * The ray buffer lives in a fixed array built into the library:
+ * rle_render_frame_noalloc_limit() bytes (64 MiB) on every device that loads
+ * the library, held until the process exits.  A frame needs
+ * 8 x rays x samples bytes of it (e.g. 1080p with up to ~4300 column rays);
+ * larger frames return RLE_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address (with that
+ * device current); make that first call before any stream capture.
+ * All calls share the one array: calls whose work can overlap on the GPU
+ * (different streams, or host threads without ordering) race -- issue them on
+ * one stream.  Nothing in the array needs clearing: every word a frame reads
+ * is written by that frame first. */
+size_t rle_render_frame_noalloc_limit(void);
+rle_status rle_render_frame_noalloc(const rle_scene* scene, const rle_camera* cam,
+                                    const rle_view_params* view, uint32_t* d_colour, float* d_depth,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

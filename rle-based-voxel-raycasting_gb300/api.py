@@ -124,6 +124,8 @@ def _load() -> C.CDLL:
         "rle_resolve": (C.c_int, [C.POINTER(RayMap), vp, vp, vp, vp, vp, vp, vp]),
         "rle_frame_workspace_bytes": (C.c_size_t, [C.POINTER(ViewParams)]),
         "rle_render_frame": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, C.c_size_t, vp, vp, vp, vp]),
+        "rle_render_frame_noalloc_limit": (C.c_size_t, []),
+        "rle_render_frame_noalloc": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -316,6 +318,18 @@ def render_frame(scene: Scene, cam: Camera, view: ViewParams, workspace, workspa
                  hit=None, stream: int = 0) -> None:
     _check(_lib.rle_render_frame(scene.handle, C.byref(cam), C.byref(view), ptr(workspace), workspace_bytes,
                                  ptr(colour), ptr(depth), ptr(hit), stream or None), "rle_render_frame")
+
+
+def render_frame_noalloc(scene: Scene, cam: Camera, view: ViewParams, colour, depth, stream: int = 0) -> None:
+    """rle_render_frame for callers that may not allocate device memory: the
+    ray buffer is a fixed array inside the library (render_frame_noalloc_limit()
+    bytes per device).  Calls share that array, so keep them on one stream."""
+    _check(_lib.rle_render_frame_noalloc(scene.handle, C.byref(cam), C.byref(view), ptr(colour), ptr(depth),
+                                         stream or None), "rle_render_frame_noalloc")
+
+
+def render_frame_noalloc_limit() -> int:
+    return int(_lib.rle_render_frame_noalloc_limit())
 
 
 def ground_height(table: np.ndarray, slabs: np.ndarray, sx: int, sy: int, x: int, z: int) -> int:
