@@ -242,6 +242,10 @@ def run_ours(args):
     e2e_ms = e0.elapsed_time(e1)
     e2e = W * H * args.steps / (e2e_ms / 1e3) / 1e6
 
+    batched = None
+    if not args.no_batch:
+        batched = run_batched(rle, torch, scene, lv0)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(rle, data, cams[args.warmup:args.warmup + max(1, min(args.cpu_frames, args.steps))])
@@ -282,12 +286,81 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if batched:
+        line["batched_vs_plain"] = batched
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line))
     return 0
+
+
+BATCH_RES = [(320, 240), (640, 480), (1280, 720), (1920, 1080)]
+
+
+def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
+    """Config 3: 64 cameras with resolutions drawn from BATCH_RES and poses
+    as config 2, rendered (a) as 64 plain per-frame launches in sequence and
+    (b) as one batched launch (tuning picked by the autotuner).  Both timed
+    with CUDA events on one stream; primary rays = pixels of all 64 frames."""
+    rng = np.random.default_rng(seed)
+    cams = poses(rle, lv0, n_cams, seed=seed)
+    views = [rle.view_params(*BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]) for _ in range(n_cams)]
+    pixels = sum(v.width * v.height for v in views)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    outs = []
+    reqs = []
+    for c, v in zip(cams, views):
+        col = torch.empty(v.width * v.height, dtype=torch.int32, device="cuda")
+        dep = torch.empty(v.width * v.height, dtype=torch.float32, device="cuda")
+        outs.append((col, dep))
+        reqs.append(rle.frame_request(c, v, col, dep))
+    ws_bytes = max(rle.frame_workspace_bytes(v) for v in views)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+
+    def plain():
+        for c, v, (col, dep) in zip(cams, views, outs):
+            rle.render_frame(scene, c, v, ws, ws_bytes, col, dep, None, stream=sp)
+
+    batch = rle.Batch(max_frames=n_cams, raybuf_words=rle.batch_words_needed(reqs), max_samples=1920)
+    t_tune = time.perf_counter()
+    best, best_ms = batch.autotune(scene, reqs, repeats=2)
+    t_tune = time.perf_counter() - t_tune
+
+    def batched():
+        batch.render(scene, reqs, stream=sp)
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(repeats):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                a.record(stream)
+                fn()
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+
+    plain_ms = timed(plain)
+    batch_ms = timed(batched)
+    batch.free()
+    return {
+        "workload": f"config 3: {n_cams} cameras, resolutions U{{320x240,640x480,1280x720,1920x1080}}, "
+                    f"config-2 poses, {pixels} pixels per batch",
+        "plain_sequential": {"value": round(pixels / plain_ms / 1e3, 1), "unit": "Mrays/s", "ms": round(plain_ms, 3)},
+        "batched": {"value": round(pixels / batch_ms / 1e3, 1), "unit": "Mrays/s", "ms": round(batch_ms, 3),
+                    "launches_per_batch": 2, "cuda_graph": True},
+        "speedup": round(plain_ms / batch_ms, 3),
+        "autotuned": {"tile_rays": best.tile_rays, "lanes_per_ray": best.lanes_per_ray, "staging": best.staging,
+                      "threads_per_block": best.threads_per_block, "tune_s": round(t_tune, 2)},
+    }
 
 
 def cpu_baseline(rle, data, cams):
@@ -365,6 +438,7 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the config-3 batched-vs-plain comparison")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -237,6 +237,55 @@ rle_status rle_render_frame(const rle_scene* scene, const rle_camera* cam,
                             size_t workspace_bytes, uint32_t* d_colour, float* d_depth,
                             rle_hit* d_hit, void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Batched rendering                                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Many cameras -- any mix of resolutions -- rendered by one persistent
+ * raycast launch and one resolve launch: the column rays of all frames form
+ * one work queue that lane groups drain tile by tile, so short and long rays
+ * of every frame balance across the GPU.  The two launches (and the upload
+ * of the per-frame parameters) are captured once into a CUDA graph and
+ * replayed for every batch.  No counterpart in the reference, which renders
+ * one camera per launch (src/Cuda_Main.cu:183-271). */
+typedef struct rle_batch rle_batch;
+
+typedef struct rle_frame_request {
+    rle_camera cam;
+    rle_view_params view;
+    uint32_t* d_colour;  /* width*height RGBA8, as rle_resolve */
+    float* d_depth;      /* width*height */
+    rle_hit* d_hit;      /* optional; needs a batch created with hits */
+} rle_frame_request;
+
+typedef struct rle_batch_tuning {
+    int tile_rays;          /* rays per work tile: 1..256 (autotuned over 8, 16, 32, 64) */
+    int lanes_per_ray;      /* lanes cooperating on one column ray: 8, 16, 32 */
+    int staging;            /* staging depth: tiles a lane group claims per grab, 1..8 */
+    int threads_per_block;  /* 32, 64, 96 or 128 */
+    int use_graph;          /* 1: capture once and replay (default); 0: plain launches */
+} rle_batch_tuning;
+
+/* max_frames per batch; raybuf_words: ray-buffer capacity shared by the
+ * frames of one batch (a frame needs rays * samples words, see
+ * rle_batch_words_needed); max_samples: largest samples-per-ray accepted. */
+rle_status rle_batch_create(int device, int max_frames, size_t raybuf_words, int max_samples, int with_hits,
+                            rle_batch** out);
+rle_status rle_batch_free(rle_batch* b);
+rle_status rle_batch_set_tuning(rle_batch* b, const rle_batch_tuning* t);
+rle_status rle_batch_get_tuning(const rle_batch* b, rle_batch_tuning* t);
+/* Ray-buffer words a set of frames needs (0 if a camera or view is invalid). */
+size_t rle_batch_words_needed(const rle_frame_request* frames, int n);
+/* Renders n frames; outputs as rle_render_frame.  Asynchronous on `stream`;
+ * one batch object renders one batch at a time (calls are serialised). */
+rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
+                            void* stream);
+/* Times every tile_rays x lanes_per_ray x staging combination
+ * ({8,16,32,64} x {8,16,32} x {1,2,3}) on these frames (median of `repeats`
+ * runs each), keeps the fastest as the batch's tuning and returns it. */
+rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
+                              int repeats, rle_batch_tuning* best, float* best_ms);
+
 /* Camera to screen without any device allocation (no counterpart in the
  * reference).  For callers that may not allocate device memory while they
  * run -- a render loop with a hard frame budget (cudaMalloc can synchronise

@@ -84,6 +84,19 @@ class Tuning(C.Structure):
 RAYCAST_SHAPES = [(8, 1), (16, 1), (32, 1)]
 
 
+class FrameRequest(C.Structure):
+    _fields_ = [("cam", Camera), ("view", ViewParams), ("d_colour", C.c_void_p), ("d_depth", C.c_void_p),
+                ("d_hit", C.c_void_p)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("tile_rays", C.c_int), ("lanes_per_ray", C.c_int), ("staging", C.c_int),
+                ("threads_per_block", C.c_int), ("use_graph", C.c_int)]
+
+    def as_tuple(self):
+        return (self.tile_rays, self.lanes_per_ray, self.staging, self.threads_per_block, self.use_graph)
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("device", C.c_int), ("nummaps", C.c_int), ("sx", C.c_int * RLE_MAX_MIPS),
                 ("sy", C.c_int * RLE_MAX_MIPS), ("sz", C.c_int * RLE_MAX_MIPS),
@@ -124,6 +137,14 @@ def _load() -> C.CDLL:
         "rle_resolve": (C.c_int, [C.POINTER(RayMap), vp, vp, vp, vp, vp, vp, vp]),
         "rle_frame_workspace_bytes": (C.c_size_t, [C.POINTER(ViewParams)]),
         "rle_render_frame": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, C.c_size_t, vp, vp, vp, vp]),
+        "rle_batch_create": (C.c_int, [C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int, C.POINTER(vp)]),
+        "rle_batch_free": (C.c_int, [vp]),
+        "rle_batch_set_tuning": (C.c_int, [vp, C.POINTER(BatchTuning)]),
+        "rle_batch_get_tuning": (C.c_int, [vp, C.POINTER(BatchTuning)]),
+        "rle_batch_words_needed": (C.c_size_t, [C.POINTER(FrameRequest), C.c_int]),
+        "rle_batch_render": (C.c_int, [vp, vp, C.POINTER(FrameRequest), C.c_int, vp]),
+        "rle_batch_autotune": (C.c_int, [vp, vp, C.POINTER(FrameRequest), C.c_int, C.c_int, C.POINTER(BatchTuning),
+                                         C.POINTER(C.c_float)]),
         "rle_render_frame_noalloc_limit": (C.c_size_t, []),
         "rle_render_frame_noalloc": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, vp, vp]),
     }
@@ -318,6 +339,72 @@ def render_frame(scene: Scene, cam: Camera, view: ViewParams, workspace, workspa
                  hit=None, stream: int = 0) -> None:
     _check(_lib.rle_render_frame(scene.handle, C.byref(cam), C.byref(view), ptr(workspace), workspace_bytes,
                                  ptr(colour), ptr(depth), ptr(hit), stream or None), "rle_render_frame")
+
+
+def frame_request(cam: Camera, view: ViewParams, colour, depth, hit=None) -> FrameRequest:
+    return FrameRequest(cam, view, ptr(colour), ptr(depth), ptr(hit))
+
+
+def _requests(frames) -> tuple:
+    arr = (FrameRequest * len(frames))(*frames)
+    return arr, len(frames)
+
+
+def batch_words_needed(frames) -> int:
+    arr, n = _requests(frames)
+    return int(_lib.rle_batch_words_needed(arr, n))
+
+
+class Batch:
+    """Many cameras per launch (rle_batch_*): one persistent raycast and one
+    persistent resolve, captured into a CUDA graph and replayed."""
+
+    def __init__(self, max_frames: int, raybuf_words: int, max_samples: int = 4096, with_hits: bool = False,
+                 device: int = 0):
+        h = C.c_void_p()
+        _check(_lib.rle_batch_create(device, max_frames, raybuf_words, max_samples, int(with_hits), C.byref(h)),
+               "rle_batch_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise RLEError(-1, "Batch", "batch was freed")
+        return self._h
+
+    def tuning(self) -> BatchTuning:
+        t = BatchTuning()
+        _check(_lib.rle_batch_get_tuning(self.handle, C.byref(t)), "rle_batch_get_tuning")
+        return t
+
+    def set_tuning(self, tile_rays: int, lanes_per_ray: int, staging: int = 1, threads_per_block: int = 128,
+                   use_graph: bool = True) -> None:
+        t = BatchTuning(tile_rays, lanes_per_ray, staging, threads_per_block, int(use_graph))
+        _check(_lib.rle_batch_set_tuning(self.handle, C.byref(t)), "rle_batch_set_tuning")
+
+    def render(self, scene: Scene, frames, stream: int = 0) -> None:
+        arr, n = _requests(frames)
+        _check(_lib.rle_batch_render(self.handle, scene.handle, arr, n, stream or None), "rle_batch_render")
+
+    def autotune(self, scene: Scene, frames, repeats: int = 3) -> tuple[BatchTuning, float]:
+        arr, n = _requests(frames)
+        best = BatchTuning()
+        ms = C.c_float()
+        _check(_lib.rle_batch_autotune(self.handle, scene.handle, arr, n, repeats, C.byref(best), C.byref(ms)),
+               "rle_batch_autotune")
+        return best, ms.value
+
+    def free(self) -> None:
+        if self._h:
+            _check(_lib.rle_batch_free(self._h), "rle_batch_free")
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.rle_batch_free(self._h)
+        except Exception:
+            pass
 
 
 def render_frame_noalloc(scene: Scene, cam: Camera, view: ViewParams, colour, depth, stream: int = 0) -> None:

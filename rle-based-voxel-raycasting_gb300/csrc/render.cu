@@ -489,26 +489,18 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
     return false;
 }
 
-// G lanes per ray; chunks of G DDA steps, lane k taking step k of each.
+// Casts ray x of frame P with the G lanes of one group (lane k, lane mask
+// gmask), using mask_words (S/32 words of shared memory) as its bitmask.
+// active = false: the lanes only take part in the group's collectives.
+// chunks of G DDA steps, lane k taking step k of each.
 template <int G>
-__global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ RayParams P) {
-    constexpr int kGroups = 32 / G;
-    extern __shared__ uint32_t smem[];
-    const int lane = threadIdx.x & 31;
-    const int g = lane / G;   // ray group within the warp
-    const int k = lane % G;   // lane within the group
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (g * G));
-    const int warp_in_block = threadIdx.x >> 5;
-    const int rays_per_block = (blockDim.x >> 5) * kGroups;
-    const int slot = warp_in_block * kGroups + g;  // ray slot within the block
-    const int x = blockIdx.x * rays_per_block + slot;
+__device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, int k,
+                                         unsigned gmask, Counts& cnt) {
     const int S = P.S;
     const int words = (S + 31) >> 5;
     const bool hits = P.rayhit != nullptr;
     const bool count = P.counters != nullptr;
-    Mask mask{smem + slot * words};
-    Counts cnt;
-    const bool active = x < P.rays;
+    Mask mask{mask_words};
 
     Ray R;
     Walk W;
@@ -664,13 +656,76 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
             }
         }
     }
-    if (count) {
-        unsigned long long v[6] = {cnt.cells, cnt.fetched, cnt.headers, cnt.runs, cnt.spans, cnt.pixels};
-        for (int i = 0; i < 6; i++) {
-            // the lanes of a group hold the same counts: take lane 0's
-            unsigned long long s = (k == 0) ? v[i] : 0ull;
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0 && s) atomicAdd(&reinterpret_cast<unsigned long long*>(P.counters)[i], s);
+    if (count && active && k == 0) {
+        // the lanes of a group hold the same counts; lane 0 adds the ray's
+        unsigned long long* c = reinterpret_cast<unsigned long long*>(P.counters);
+        const unsigned long long v[6] = {cnt.cells, cnt.fetched, cnt.headers, cnt.runs, cnt.spans, cnt.pixels};
+        for (int i = 0; i < 6; i++)
+            if (v[i]) atomicAdd(&c[i], v[i]);
+    }
+    cnt = Counts();
+}
+
+// Lane layout of a group of G lanes within a block.
+template <int G>
+struct Lanes {
+    int lane, g, k, slot;
+    unsigned gmask;
+    __device__ __forceinline__ Lanes() {
+        constexpr int kGroups = 32 / G;
+        lane = threadIdx.x & 31;
+        g = lane / G;  // ray group within the warp
+        k = lane % G;  // lane within the group
+        gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (g * G));
+        slot = (threadIdx.x >> 5) * kGroups + g;  // ray slot within the block
+    }
+};
+
+// One frame: ray slot s of block b casts ray b * slots + s.
+template <int G>
+__global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ RayParams P) {
+    extern __shared__ uint32_t smem[];
+    const Lanes<G> L;
+    const int rays_per_block = (blockDim.x >> 5) * (32 / G);
+    const int x = blockIdx.x * rays_per_block + L.slot;
+    const int words = (P.S + 31) >> 5;
+    Counts cnt;
+    cast_ray<G>(P, x, x < P.rays, smem + L.slot * words, L.k, L.gmask, cnt);
+}
+
+// Many frames in one persistent launch.  The rays of all frames form one
+// index space (ray_start[f] = first global ray of frame f); each group takes
+// `tile` consecutive rays at a time from a global counter until none are
+// left, so long and short rays of every frame balance across the GPU.
+template <int G>
+__global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, const int* __restrict__ ray_start,
+                                                            const RayParams* __restrict__ frames, int tile,
+                                                            int staging, int max_words) {
+    extern __shared__ uint32_t smem[];
+    const Lanes<G> L;
+    const int nframes = hdr->nframes;
+    const int total = ray_start[nframes];
+    uint32_t* mask_words = smem + L.slot * max_words;
+    Counts cnt;
+    int f = 0;  // frame of the current ray (rays are taken in increasing order)
+    const int grab = tile * staging;  // staging depth: tiles a group claims at once
+    for (;;) {
+        unsigned int t0 = 0;
+        if (L.k == 0) t0 = atomicAdd(&hdr->next_ray, static_cast<unsigned int>(grab));
+        t0 = __shfl_sync(L.gmask, t0, lane_base(L.gmask));
+        if (static_cast<int>(t0) >= total) break;
+        const int t1 = min(static_cast<int>(t0) + grab, total);
+        for (int r = static_cast<int>(t0); r < t1; r++) {
+            if (r < ray_start[f] || r >= ray_start[f + 1]) {
+                int lo = 0, hi = nframes - 1;  // last frame with ray_start <= r
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (ray_start[mid] <= r) lo = mid;
+                    else hi = mid - 1;
+                }
+                f = lo;
+            }
+            cast_ray<G>(frames[f], r - ray_start[f], true, mask_words, L.k, L.gmask, cnt);
         }
     }
 }
@@ -700,7 +755,79 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
     return RLE_OK;
 }
 
+template <int G>
+size_t batch_smem(int threads, int max_samples) {
+    return static_cast<size_t>(threads / 32 * (32 / G)) * ((max_samples + 31) >> 5) * 4;
+}
+
+template <int G>
+rle_status batch_blocks(int threads, int max_samples, int* blocks) {
+    const size_t smem = batch_smem<G>(threads, max_samples);
+    if (smem > 227 * 1024) {
+        set_error("batch: %d samples per ray exceed shared memory at this launch shape", max_samples);
+        return RLE_ERR_CAPACITY;
+    }
+    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    int dev = 0, sms = 0, per_sm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G>, threads, smem);
+    if (e != cudaSuccess) {
+        set_error("batch launch set-up: %s", cudaGetErrorString(e));
+        return RLE_ERR_CUDA;
+    }
+    *blocks = sms * (per_sm > 0 ? per_sm : 1);
+    return RLE_OK;
+}
+
+template <int G>
+rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
+    const size_t smem = batch_smem<G>(b.threads, b.max_samples);
+    int blocks = b.blocks;
+    if (blocks <= 0) {
+        const rle_status st = batch_blocks<G>(b.threads, b.max_samples, &blocks);
+        if (st != RLE_OK) return st;
+    }
+    raycast_batch_kernel<G><<<blocks, b.threads, smem, stream>>>(b.header, b.ray_start, b.frames, b.tile,
+                                                                 b.staging, (b.max_samples + 31) >> 5);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("batch raycast launch: %s", cudaGetErrorString(e));
+        return RLE_ERR_CUDA;
+    }
+    return RLE_OK;
+}
+
 }  // namespace
+
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks) {
+    switch (lanes) {
+        case 8: return batch_blocks<8>(threads, max_samples, blocks);
+        case 16: return batch_blocks<16>(threads, max_samples, blocks);
+        case 32: return batch_blocks<32>(threads, max_samples, blocks);
+        default:
+            set_error("batch: lanes per ray must be 8, 16 or 32");
+            return RLE_ERR_INVALID_ARG;
+    }
+}
+
+rle_status launch_raycast_batch(const BatchRaycast& b, void* stream) {
+    if (b.threads % 32 != 0 || b.threads <= 0 || b.threads > 128 || b.tile < 1 || b.staging < 1) {
+        set_error("batch: threads per block a multiple of 32 up to 128, tile >= 1, staging >= 1");
+        return RLE_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    switch (b.lanes) {
+        case 8: return batch_launch<8>(b, s);
+        case 16: return batch_launch<16>(b, s);
+        case 32: return batch_launch<32>(b, s);
+        default:
+            set_error("batch: lanes per ray must be 8, 16 or 32");
+            return RLE_ERR_INVALID_ARG;
+    }
+}
 
 rle_status launch_raycast(const RayParams& p, void* stream) {
     if (p.rays <= 0) return RLE_OK;

@@ -34,10 +34,7 @@ __device__ __forceinline__ uint32_t rgb565_to_rgba8(uint32_t c) {
 }
 
 template <bool kHits>
-__global__ void resolve_kernel(const __grid_constant__ ResolveParams P) {
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y;
-    if (col >= P.width || row >= P.height) return;
+__device__ __forceinline__ void resolve_pixel(const ResolveParams& P, int col, int row) {
     const float RESX = P.resx, RESY = P.resy;
     const float fx = static_cast<float>(col) + 0.5f;
     const float fy = static_cast<float>(P.height - 1 - row) + 0.5f;  // GL rows count from the bottom
@@ -98,7 +95,61 @@ __global__ void resolve_kernel(const __grid_constant__ ResolveParams P) {
     }
 }
 
+template <bool kHits>
+__global__ void resolve_kernel(const __grid_constant__ ResolveParams P) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y;
+    if (col >= P.width || row >= P.height) return;
+    resolve_pixel<kHits>(P, col, row);
+}
+
+// All frames of a batch: block b belongs to the frame f with
+// block_start[f] <= b < block_start[f+1] and covers 256 of its pixels.
+constexpr int kResolveBlock = 256;
+
+// Persistent: block i takes pixel blocks i, i + gridDim.x, ... of the batch.
+__global__ void __launch_bounds__(kResolveBlock) resolve_batch_kernel(const BatchHeader* __restrict__ hdr,
+                                                                      const int* __restrict__ block_start,
+                                                                      const ResolveParams* __restrict__ frames) {
+    const int nframes = hdr->nframes;
+    const int total = block_start[nframes];
+    int f = 0;
+    for (int b = blockIdx.x; b < total; b += gridDim.x) {
+        if (b < block_start[f] || b >= block_start[f + 1]) {
+            int lo = 0, hi = nframes - 1;  // last frame with block_start <= b
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (block_start[mid] <= b) lo = mid;
+                else hi = mid - 1;
+            }
+            f = lo;
+        }
+        const ResolveParams& P = frames[f];
+        const long long pix = static_cast<long long>(b - block_start[f]) * kResolveBlock + threadIdx.x;
+        if (pix >= static_cast<long long>(P.width) * P.height) continue;
+        const int row = static_cast<int>(pix / P.width), col = static_cast<int>(pix % P.width);
+        if (P.hit) resolve_pixel<true>(P, col, row);
+        else resolve_pixel<false>(P, col, row);
+    }
+}
+
 }  // namespace
+
+int resolve_batch_blocks(int width, int height) {
+    return static_cast<int>((static_cast<long long>(width) * height + kResolveBlock - 1) / kResolveBlock);
+}
+
+rle_status launch_resolve_batch(const BatchResolve& b, void* stream) {
+    if (b.blocks <= 0) return RLE_OK;
+    resolve_batch_kernel<<<b.blocks, kResolveBlock, 0, static_cast<cudaStream_t>(stream)>>>(b.header, b.block_start,
+                                                                                            b.frames);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("batch resolve launch: %s", cudaGetErrorString(e));
+        return RLE_ERR_CUDA;
+    }
+    return RLE_OK;
+}
 
 rle_status launch_resolve(const ResolveParams& p, void* stream) {
     const dim3 block(128, 1, 1);

@@ -105,4 +105,34 @@ rle_status fill_resolve_params(const rle_raymap* rm, ResolveParams* p);
 rle_status launch_raycast(const RayParams& p, void* stream);
 rle_status launch_resolve(const ResolveParams& p, void* stream);
 
+// Many frames in one launch each (batch.cpp drives these).  The frame count
+// and the work counter live in device memory, so one captured graph serves
+// every batch size.
+struct BatchHeader {
+    int nframes;
+    unsigned int next_ray;     // work counter, zero before the launch
+    int pad[2];
+};
+struct BatchRaycast {
+    BatchHeader* header;       // device
+    const int* ray_start;      // device array [nframes + 1], prefix of rays
+    const RayParams* frames;   // device array [nframes]
+    int tile;                  // rays per tile
+    int staging;               // tiles a group claims per grab
+    int lanes;                 // lanes per ray: 8, 16, 32
+    int threads;               // block size
+    int max_samples;           // largest S of the frames the launch may see
+    int blocks;                // grid size (0: fill the GPU)
+};
+struct BatchResolve {
+    const BatchHeader* header;    // device
+    const int* block_start;       // device array [nframes + 1], prefix of 256-pixel blocks
+    const ResolveParams* frames;  // device array [nframes]
+    int blocks;                   // persistent grid size
+};
+rle_status launch_raycast_batch(const BatchRaycast& b, void* stream);
+rle_status launch_resolve_batch(const BatchResolve& b, void* stream);
+int resolve_batch_blocks(int width, int height);  // 256-pixel blocks of one frame
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks);
+
 }  // namespace rle

@@ -1,0 +1,147 @@
+"""Batched rendering (rle_batch_*): many cameras of mixed resolution in one
+persistent raycast + resolve, replayed from a captured CUDA graph.  Every
+frame must equal the same camera rendered alone by rle_render_frame, bit for
+bit, for every launch shape, with and without the graph, across consecutive
+batches of different sizes."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RES = [(160, 120), (320, 240), (640, 480), (200, 200), (400, 225)]
+
+
+@pytest.fixture(scope="module")
+def scene(rle, torch_cuda):
+    data = rle.scenegen_rle4(rle.scenegen_default(256, 256, 256, 4, caves=True))
+    s = rle.Scene.from_bytes(data)
+    yield s
+    s.free()
+
+
+def _cameras(rle, scene, n, seed):
+    info = scene.info()
+    table, words = scene.copy_level(0)
+    rng = np.random.default_rng(seed)
+    cams = []
+    for i in range(n):
+        x, z = rng.uniform(0, 256, 2)
+        g = rle.ground_height(table, words, info.sx[0], info.sy[0], int(x), int(z))
+        pitch = float(rng.uniform(2, 60) * rng.choice([-1, 1]))
+        cam = rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)), pitch)
+        w, h = RES[i % len(RES)]
+        cams.append((cam, rle.view_params(w, h, mip_distance=96)))
+    return cams
+
+
+def _alone(rle, torch, scene, cam, view):
+    n = view.width * view.height
+    ws_bytes = rle.frame_workspace_bytes(view)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    c = torch.empty(n, dtype=torch.int32, device="cuda")
+    d = torch.empty(n, dtype=torch.float32, device="cuda")
+    h = torch.empty(n * 8, dtype=torch.uint8, device="cuda")
+    rle.render_frame(scene, cam, view, ws, ws_bytes, c, d, h)
+    torch.cuda.synchronize()
+    return c.cpu().numpy().view(np.uint32), d.cpu().numpy(), h.cpu().numpy().view(rle.HIT_DTYPE)
+
+
+class Outputs:
+    def __init__(self, torch, rle, cams, hits=True):
+        self.bufs = []
+        self.reqs = []
+        for cam, view in cams:
+            n = view.width * view.height
+            c = torch.full((n,), 3, dtype=torch.int32, device="cuda")
+            d = torch.full((n,), 3.0, dtype=torch.float32, device="cuda")
+            h = torch.zeros(n * 8, dtype=torch.uint8, device="cuda") if hits else None
+            self.bufs.append((c, d, h))
+            self.reqs.append(rle.frame_request(cam, view, c, d, h))
+
+    def host(self, rle, i):
+        c, d, h = self.bufs[i]
+        return (c.cpu().numpy().view(np.uint32), d.cpu().numpy(),
+                h.cpu().numpy().view(rle.HIT_DTYPE) if h is not None else None)
+
+
+def _check(rle, torch, scene, cams, outs, label):
+    torch.cuda.synchronize()
+    for i, (cam, view) in enumerate(cams):
+        want = _alone(rle, torch, scene, cam, view)
+        got = outs.host(rle, i)
+        assert np.array_equal(got[0], want[0]), f"{label} frame {i}: {int((got[0] != want[0]).sum())} pixels differ"
+        assert np.array_equal(got[1].view(np.uint32), want[1].view(np.uint32)), f"{label} frame {i} depth"
+        if got[2] is not None:
+            assert np.array_equal(got[2], want[2]), f"{label} frame {i} hits"
+
+
+def test_batch_matches_single_frames(rle, scene, torch_cuda):
+    torch = torch_cuda
+    cams = _cameras(rle, scene, 12, 1)
+    outs = Outputs(torch, rle, cams)
+    words = rle.batch_words_needed(outs.reqs)
+    assert words > 0
+    b = rle.Batch(max_frames=16, raybuf_words=words, max_samples=1024, with_hits=True)
+    b.render(scene, outs.reqs)
+    _check(rle, torch, scene, cams, outs, "graph")
+    # replay the captured graph with another, smaller batch, then the first again
+    cams2 = _cameras(rle, scene, 5, 2)
+    outs2 = Outputs(torch, rle, cams2)
+    b.render(scene, outs2.reqs)
+    _check(rle, torch, scene, cams2, outs2, "second batch")
+    outs3 = Outputs(torch, rle, cams)
+    b.render(scene, outs3.reqs)
+    _check(rle, torch, scene, cams, outs3, "third batch")
+    b.free()
+
+
+@pytest.mark.parametrize("shape", [(1, 8, 1, 128, 1), (8, 16, 3, 64, 1), (64, 32, 2, 128, 0), (16, 32, 1, 32, 1)])
+def test_batch_shapes(rle, scene, torch_cuda, shape):
+    torch = torch_cuda
+    cams = _cameras(rle, scene, 7, 3)
+    outs = Outputs(torch, rle, cams, hits=False)
+    b = rle.Batch(max_frames=8, raybuf_words=rle.batch_words_needed(outs.reqs), max_samples=1024)
+    b.set_tuning(*shape)
+    assert b.tuning().as_tuple() == shape
+    b.render(scene, outs.reqs)
+    b.render(scene, outs.reqs)  # twice in a row on the same outputs
+    _check(rle, torch, scene, cams, outs, f"shape {shape}")
+    b.free()
+
+
+def test_batch_refuses_what_it_cannot_hold(rle, scene, torch_cuda):
+    torch = torch_cuda
+    cams = _cameras(rle, scene, 3, 4)
+    outs = Outputs(torch, rle, cams)
+    words = rle.batch_words_needed(outs.reqs)
+    small = rle.Batch(max_frames=4, raybuf_words=words // 2, max_samples=1024, with_hits=True)
+    with pytest.raises(rle.RLEError) as e:
+        small.render(scene, outs.reqs)
+    assert e.value.name == "RLE_ERR_CAPACITY"
+    nohits = rle.Batch(max_frames=4, raybuf_words=words, max_samples=1024, with_hits=False)
+    with pytest.raises(rle.RLEError):
+        nohits.render(scene, outs.reqs)  # hit outputs asked of a batch without hit storage
+    narrow = rle.Batch(max_frames=4, raybuf_words=words, max_samples=256, with_hits=True)
+    with pytest.raises(rle.RLEError) as e:
+        narrow.render(scene, outs.reqs)  # 640-wide frame: 640 samples per ray
+    assert e.value.name == "RLE_ERR_CAPACITY"
+    with pytest.raises(rle.RLEError):
+        rle.Batch(max_frames=2, raybuf_words=words, max_samples=1024).render(scene, outs.reqs)  # too many frames
+    for b in (small, nohits, narrow):
+        b.free()
+
+
+def test_autotune_picks_a_valid_shape(rle, scene, torch_cuda):
+    torch = torch_cuda
+    cams = _cameras(rle, scene, 6, 5)
+    outs = Outputs(torch, rle, cams, hits=False)
+    b = rle.Batch(max_frames=8, raybuf_words=rle.batch_words_needed(outs.reqs), max_samples=1024)
+    best, ms = b.autotune(scene, outs.reqs, repeats=1)
+    assert best.tile_rays in (8, 16, 32, 64) and best.lanes_per_ray in (8, 16, 32) and best.staging in (1, 2, 3)
+    assert ms > 0
+    assert b.tuning().as_tuple() == best.as_tuple()
+    b.render(scene, outs.reqs)
+    _check(rle, torch, scene, cams, outs, "autotuned")
+    b.free()
