@@ -65,6 +65,8 @@ rle_status fill_ray_params(const rle_scene* scene, const rle_raymap* rm, RayPara
     p->nummaps = scene->nummaps;
     p->gridx0 = scene->lv[0].sx;
     p->gridz0 = scene->lv[0].sz;
+    p->top_index = scene->top_index;
+    p->height = scene->height;
     for (int m = 0; m < scene->nummaps; m++) {
         p->table[m] = reinterpret_cast<const uint2*>(scene->lv[m].d_table);
         p->slabs[m] = scene->lv[m].d_slabs;

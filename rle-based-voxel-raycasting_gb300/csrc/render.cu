@@ -489,6 +489,35 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
     return false;
 }
 
+// Whether no cell at or beyond DDA distance t0 can draw a span.
+//
+// A run whose top lies h below the eye (h = position.y + its column index,
+// level-0 units, h grows downwards) seen at distance t projects with
+// pz1 = c*t + d*h and py1 = py_t*t + py_h*h (c = cos_x*ray_z, d = sin_x;
+// py_t = -rmul*sin_x*ray_z, py_h = rmul*cos_x for rays of the up/down fans,
+// py_t = rmul*ray_x, py_h = 0 for the left/right fans; :483-559).  The run is
+// dropped at its turn (`scr_y2 <= ymin`, or `pz1 <= 0`) whenever
+// f = K*pz1 + py1 < 0 with K = res_y2 - ymin - 1.  f is linear in (t, h), so
+// it stays negative for every t >= t0 and every h >= h0 (h0: the scene's
+// topmost voxel) if its slopes in t and h are not positive and f(t0, h0) < 0.
+// A margin of 1e-4 of the magnitudes of the terms covers the float rounding
+// of the kernel's evaluation (about 1e-6 relative); ymin only grows later,
+// which only lowers f where pz1 > 0.
+__device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, float t0, int ymin) {
+    const float eps = 1e-4f;
+    const float res_y2 = static_cast<float>(P.S / 2);
+    const float K = res_y2 - static_cast<float>(ymin) - 1.0f;
+    const float c = P.cos_x * R.ray_z, d = P.sin_x;
+    const float py_t = R.vertical ? -R.rmul * P.sin_x * R.ray_z : R.rmul * R.ray_x;
+    const float py_h = R.vertical ? R.rmul * P.cos_x : 0.0f;
+    const float a = K * c + py_t, b = K * d + py_h;
+    const float scale = res_y2 + fabsf(K) + 1.0f;
+    const float ma = fabsf(c) * scale + fabsf(py_t), mb = fabsf(d) * scale + fabsf(py_h);
+    const float h0 = P.posy + static_cast<float>(P.top_index);
+    return a + eps * ma <= 0.0f && b + eps * mb <= 0.0f &&
+           a * t0 + b * h0 + eps * (ma * t0 + mb * fabsf(h0)) < 0.0f;
+}
+
 // Casts ray x of frame P with the G lanes of one group (lane k, lane mask
 // gmask), using mask_words (S/32 words of shared memory) as its bitmask.
 // active = false: the lanes only take part in the group's collectives.
@@ -639,6 +668,11 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                 merge_cell<G>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, cnt, count);
             }
             if (stop || ymin >= ymax || ended) break;
+            // Nothing further along this ray can be drawn once every run of
+            // every later cell projects below the floating horizon (the
+            // reference walks on to z_far without drawing).  Exact counters
+            // need the full walk, so they keep it.
+            if (!count && ray_is_done(P, R, W.d.dd_now, ymin)) break;
         }
     }
     __syncwarp();

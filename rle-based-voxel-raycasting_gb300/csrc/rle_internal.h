@@ -34,6 +34,10 @@ struct rle_scene {
     uint64_t device_bytes = 0;
     uint64_t run_headers = 0;
     uint64_t surface_voxels = 0;
+    // smallest column-axis index (level-0 units) of any stored voxel on any
+    // level: nothing in the scene lies above it
+    int top_index = 0;
+    int height = 0;  // sy of level 0
 };
 
 namespace rle {
@@ -46,7 +50,7 @@ struct HostLevel {
 };
 rle_status parse_rle4(const void* bytes, size_t nbytes, HostLevel* levels, int* nummaps);
 rle_status build_table(const HostLevel& lv, uint32_t* table, uint64_t* run_headers,
-                       uint64_t* surface_voxels);
+                       uint64_t* surface_voxels, int* top_index = nullptr);
 
 // Kernel parameters of one ray map bound to one scene.  Everything the
 // device needs per frame, passed by value as a __grid_constant__.
@@ -67,6 +71,8 @@ struct RayParams {
     int z_far;
     int nummaps;
     int gridx0, gridz0;
+    int top_index;                // scene's topmost voxel index (level-0 units)
+    int height;                   // scene height (level 0)
     const uint2* table[RLE_MAX_MIPS];
     const uint16_t* slabs[RLE_MAX_MIPS];
     uint32_t* raybuf;

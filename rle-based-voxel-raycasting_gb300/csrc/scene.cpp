@@ -97,10 +97,11 @@ rle_status parse_rle4(const void* bytes, size_t nbytes, HostLevel* levels, int* 
 }
 
 rle_status build_table(const HostLevel& lv, uint32_t* table, uint64_t* run_headers,
-                       uint64_t* surface_voxels) {
+                       uint64_t* surface_voxels, int* top_index) {
     const uint16_t* s = lv.slabs;
     const uint64_t words = lv.words;
     uint64_t ofs = 0, heads = 0, vox = 0;
+    uint64_t top = UINT64_MAX;  // smallest index of a stored voxel
     for (int z = 0; z < lv.sz; z++) {
         for (int x = 0; x < lv.sx; x++) {
             if (ofs + 2 > words) {
@@ -115,8 +116,19 @@ rle_status build_table(const HostLevel& lv, uint32_t* table, uint64_t* run_heade
                 return RLE_ERR_FORMAT;
             }
             // Colours the run headers address (solid counts) must exist.
-            uint64_t claimed = 0;
-            for (uint32_t r = 0; r < runs; r++) claimed += s[ofs + 2 + r] >> 10;
+            uint64_t claimed = 0, depth = 0;
+            bool found = false;
+            for (uint32_t r = 0; r < runs; r++) {
+                const uint32_t h = s[ofs + 2 + r];
+                claimed += h >> 10;
+                if (!found) {
+                    depth += h & 1023u;
+                    if (h >> 10) {
+                        found = true;
+                        if (depth < top) top = depth;
+                    }
+                }
+            }
             if (claimed > colours) {
                 set_error(".rle4: column (%d,%d) runs need %llu colours, %u stored", x, z,
                           static_cast<unsigned long long>(claimed), colours);
@@ -139,6 +151,7 @@ rle_status build_table(const HostLevel& lv, uint32_t* table, uint64_t* run_heade
     }
     if (run_headers) *run_headers = heads;
     if (surface_voxels) *surface_voxels = vox;
+    if (top_index) *top_index = top > 0x7fffffffull ? 0x7fffffff : static_cast<int>(top);
     return RLE_OK;
 }
 
@@ -183,6 +196,7 @@ extern "C" rle_status rle_scene_load_memory(const void* bytes, size_t nbytes, in
     // device work, so malformed input never reaches the GPU.
     std::vector<std::vector<uint32_t>> tables(nummaps);
     uint64_t heads0 = 0, vox0 = 0;
+    long long top_all = 0x7fffffffLL;
     for (int m = 0; m < nummaps; m++) {
         try {
             tables[m].resize(2 * static_cast<size_t>(levels[m].sx) * levels[m].sz);
@@ -191,12 +205,16 @@ extern "C" rle_status rle_scene_load_memory(const void* bytes, size_t nbytes, in
             return RLE_ERR_NO_MEMORY;
         }
         uint64_t heads = 0, vox = 0;
-        st = rle::build_table(levels[m], tables[m].data(), &heads, &vox);
+        int top = 0;
+        st = rle::build_table(levels[m], tables[m].data(), &heads, &vox, &top);
         if (st != RLE_OK) return st;
         if (m == 0) {
             heads0 = heads;
             vox0 = vox;
         }
+        // a voxel of level m at index j spans level-0 indices j << m onwards
+        const long long top0 = static_cast<long long>(top) << m;
+        if (top0 < top_all) top_all = top0;
     }
 
     int ndev = 0;
@@ -218,6 +236,8 @@ extern "C" rle_status rle_scene_load_memory(const void* bytes, size_t nbytes, in
         return cuda_fail(e, "cudaSetDevice");
     }
     s->run_headers = heads0;
+    s->top_index = static_cast<int>(top_all);
+    s->height = levels[0].sy;
     s->surface_voxels = vox0;
     for (int m = 0; m < nummaps && st == RLE_OK; m++) {
         const rle::HostLevel& hl = levels[m];

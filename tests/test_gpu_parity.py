@@ -69,6 +69,8 @@ def test_golden_raybuf_bit_exact(rle, po, golden, golden_scene, torch_cuda, i):
     ref = golden[f"raybuf_{i}"]
     assert words.shape == ref.shape
     assert np.array_equal(words, ref), f"{int((words != ref).sum())} of {ref.size} differ from the reference"
+    fast = Frame(torch_cuda, rle, scene, rm, hits=False, counters=False).rays_host()[0]
+    assert np.array_equal(fast, ref), "fast path (no counters) differs from the reference"
     orc, _ = _oracle_frame(po, rm, oscene)
     assert_rays_equal((words, depth, hits, cnt), orc, f"golden cam {i}")
     assert counters_dict(cnt) == oracle_counters(orc[3])
@@ -87,6 +89,8 @@ def test_config1_frame(rle, po, scene512, torch_cuda):
     orc, om = _oracle_frame(po, rm, oscene)
     assert_rays_equal(gpu, orc, "config 1")
     assert counters_dict(gpu[3]) == oracle_counters(orc[3])
+    fast = Frame(torch_cuda, rle, scene, rm, hits=True, counters=False).rays_host()
+    assert_rays_equal(fast, orc, "config 1 (no counters)")
     col, dep, hit = fr.resolve_host()
     ocol, odep, ohit, _ = po.resolve(om, 640, 480, orc[0], orc[1], orc[2])
     assert np.array_equal(col, ocol), f"{int((col != ocol).sum())} pixels differ"
@@ -121,6 +125,9 @@ def test_cave_scene_poses(rle, po, caves256, torch_cuda, pose):
     orc, om = _oracle_frame(po, rm, oscene)
     assert_rays_equal(gpu, orc, str(pose))
     assert counters_dict(gpu[3]) == oracle_counters(orc[3])
+    # without counters the kernel may stop a ray early once nothing more can draw
+    fast = Frame(torch_cuda, rle, scene, rm, hits=True, counters=False).rays_host()
+    assert_rays_equal(fast, orc, f"{pose} (no counters)")
     col, dep, hit = fr.resolve_host()
     ocol, odep, ohit, _ = po.resolve(om, W, H, orc[0], orc[1], orc[2])
     assert np.array_equal(col, ocol) and np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
@@ -144,6 +151,26 @@ def test_random_poses_many(rle, po, caves256, torch_cuda):
         assert_rays_equal(gpu, orc, f"pose {k}")
         total += gpu[0].size
     assert total > 0
+
+
+def test_config2_scene_frames(rle, po, torch_cuda):
+    """The benchmark's scene (2048^2 x 256 caves, seed 2) and camera law at
+    960x540: the fast path (early ray termination, no counters) against the
+    oracle on 10 poses, hit records included."""
+    data = rle.scenegen_rle4(rle.scenegen_default(2048, 256, 2048, 2, caves=True))
+    scene, oscene = rle.Scene.from_bytes(data), po.OracleScene.from_rle4(data)
+    t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
+    rng = np.random.default_rng(99)
+    for k in range(10):
+        x, z = rng.uniform(0, 2048, 2)
+        g = rle.ground_height(t0, s0, 2048, 256, int(x), int(z))
+        pitch = float(rng.uniform(1, 30) * rng.choice([-1, 1]))
+        cam = rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)), pitch)
+        rm = rle.raymap_build(cam, rle.view_params(960, 540))
+        gpu = Frame(torch_cuda, rle, scene, rm, hits=True, counters=False).rays_host()
+        orc, _ = _oracle_frame(po, rm, oscene)
+        assert_rays_equal(gpu, orc, f"config-2 pose {k}")
+    scene.free()
 
 
 def test_render_frame_equals_two_calls(rle, scene512, torch_cuda):
