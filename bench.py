@@ -245,6 +245,9 @@ def run_ours(args):
     batched = None
     if not args.no_batch:
         batched = run_batched(rle, torch, scene, lv0)
+    serving = None
+    if args.serve_seconds > 0:
+        serving = run_serving(rle, torch, seconds=args.serve_seconds)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -288,6 +291,8 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if batched:
         line["batched_vs_plain"] = batched
+    if serving:
+        line["serving"] = serving
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -361,6 +366,78 @@ def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
         "autotuned": {"tile_rays": best.tile_rays, "lanes_per_ray": best.lanes_per_ray, "staging": best.staging,
                       "threads_per_block": best.threads_per_block, "tune_s": round(t_tune, 2)},
     }
+
+
+SERVE_RES = [((256, 256), 0.4), ((640, 480), 0.3), ((1280, 720), 0.2), ((1920, 1080), 0.1)]
+SERVE_SCENES = [(1024, 3), (2048, 4), (2048, 5), (4096, 6)]
+
+
+def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None):
+    """Config 4: 4 resident scenes (1024^2, 2048^2, 2048^2, 4096^2 x 256,
+    seeds 3-6), Poisson arrivals at `lam` requests/s for `seconds`, each
+    request a uniform scene and a resolution from SERVE_RES, seeded poses
+    (config-2 law), HBM budget 120 GB.  Served twice -- continuous batching
+    and one launch per request -- at the same offered load, then both at
+    saturation (every request queued at once)."""
+    if scenes is None:
+        scenes = []
+        for n, s in SERVE_SCENES:
+            scenes.append(rle.Scene.from_bytes(rle.scenegen_rle4(rle.scenegen_default(n, 256, n, s, caves=True))))
+    rng = np.random.default_rng(seed)
+    levels = []
+    for sc in scenes:
+        info = sc.info()
+        t, w = sc.copy_level(0)
+        levels.append((info.sx[0], info.sy[0], info.sz[0], t, w))
+    n_req = int(lam * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, n_req))
+    probs = np.array([p for _, p in SERVE_RES])
+    reqs = []
+    for i in range(n_req):
+        sid = int(rng.integers(0, len(scenes)))
+        (w, h) = SERVE_RES[int(rng.choice(len(SERVE_RES), p=probs))][0]
+        cam = poses(rle, levels[sid], 1, seed=seed + 7 * i + 1)[0]
+        reqs.append((sid, cam, rle.view_params(w, h)))
+    ring = 64  # output buffers reused round-robin
+    outs = [(torch.empty(1920 * 1080, dtype=torch.int32, device="cuda"),
+             torch.empty(1920 * 1080, dtype=torch.float32, device="cuda")) for _ in range(ring)]
+    pixels = sum(v.width * v.height for _, _, v in reqs)
+    result = {"workload": f"config 4: 4 resident scenes (1024^2, 2048^2 x2, 4096^2 x 256), Poisson "
+                          f"{lam:g} req/s for {seconds:g} s ({n_req} requests, {pixels / n_req / 1e3:.0f} kpx mean), "
+                          f"resolution mix 256^2:.4 640x480:.3 1280x720:.2 1920x1080:.1, HBM budget 120 GB"}
+    for mode in ("batched", "plain"):
+        srv = rle.Server(hbm_budget_bytes=120 << 30, raybuf_words=32 << 20, max_frames_per_batch=64,
+                         max_inflight=3, max_samples=1920, plain=(mode == "plain"))
+        for sc in scenes:
+            srv.add_scene(sc)
+        # warm-up: one of each resolution
+        for k in range(8):
+            sid, cam, v = reqs[k]
+            srv.wait(srv.submit(sid, cam, v, outs[k][0], outs[k][1]))
+        srv.reset_stats()
+        entry = {}
+        for load in ("offered", "saturated"):
+            srv.reset_stats()
+            t0 = time.perf_counter()
+            for i, (sid, cam, v) in enumerate(reqs):
+                if load == "offered":
+                    delay = t0 + arrivals[i] - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                c, d = outs[i % ring]
+                srv.submit(sid, cam, v, c, d)
+            srv.drain(600000)
+            srv.poll(1 << 20)
+            st = srv.stats()
+            entry[load] = {"mrays_per_s": round(st.mrays_per_s, 1), "p50_ms": round(st.p50_ms, 3),
+                           "p99_ms": round(st.p99_ms, 3), "max_ms": round(st.max_ms, 3),
+                           "completed": int(st.completed), "batches": int(st.batches),
+                           "wall_s": round(time.perf_counter() - t0, 3)}
+        result[mode] = entry
+        srv.destroy()
+    result["throughput_ratio_saturated"] = round(
+        result["batched"]["saturated"]["mrays_per_s"] / max(result["plain"]["saturated"]["mrays_per_s"], 1e-9), 2)
+    return result
 
 
 def cpu_baseline(rle, data, cams):
@@ -439,6 +516,8 @@ def main(argv=None):
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the config-3 batched-vs-plain comparison")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="seconds of Poisson arrivals in the config-4 serving comparison (0: skip)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

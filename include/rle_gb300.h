@@ -286,6 +286,80 @@ rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_fram
 rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                               int repeats, rle_batch_tuning* best, float* best_ms);
 
+/* ---------------------------------------------------------------------- */
+/* Serving                                                                */
+/* ---------------------------------------------------------------------- */
+
+/* A render server: scenes stay resident on one device, requests queue on the
+ * host and a scheduler thread turns the queue into batched launches as soon
+ * as a batch slot and ray-buffer memory are free (continuous batching: work
+ * that arrives while other batches run joins the next launch, and up to
+ * max_inflight batches overlap on the device).  A request's outputs go to
+ * device buffers its submitter owns.  No counterpart in the reference,
+ * which renders one camera per call in its display loop. */
+typedef struct rle_server rle_server;
+
+typedef struct rle_server_config {
+    int device;
+    size_t hbm_budget_bytes;      /* scenes + the server's ray buffers must fit */
+    int max_frames_per_batch;     /* frames one launch may carry */
+    int max_inflight;             /* batches on the device at once (>= 1) */
+    size_t raybuf_words;          /* ray-buffer words of each batch slot */
+    int max_samples;              /* widest samples-per-ray accepted */
+    int plain;                    /* 1: one request per launch, one at a time (for comparison) */
+} rle_server_config;
+
+typedef struct rle_request {
+    int scene_id;
+    rle_camera cam;
+    rle_view_params view;
+    uint32_t* d_colour;
+    float* d_depth;
+} rle_request;
+
+typedef struct rle_completion {
+    uint64_t ticket;
+    rle_status status;
+    double submit_s, launch_s, done_s;  /* host monotonic clock, seconds */
+} rle_completion;
+
+typedef struct rle_server_stats {
+    uint64_t submitted, completed, failed, cancelled, batches;
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> done, over completed requests */
+    double pixels;                           /* primary rays rendered */
+    double busy_s;                           /* first submit -> last completion */
+    double mrays_per_s;                      /* pixels / busy_s / 1e6 */
+    uint64_t device_bytes;                   /* scenes + ray buffers held */
+} rle_server_stats;
+
+rle_status rle_server_create(const rle_server_config* cfg, rle_server** out);
+/* Registers a loaded scene (on the server's device); its device bytes count
+ * against the budget (RLE_ERR_NO_MEMORY if it does not fit). */
+rle_status rle_server_add_scene(rle_server* s, const rle_scene* scene, int* scene_id);
+/* Queues a request (non-blocking).  RLE_ERR_CAPACITY if it could never fit
+ * one batch slot; RLE_ERR_INVALID_ARG for a bad scene id, camera or view. */
+rle_status rle_server_submit(rle_server* s, const rle_request* r, uint64_t* ticket);
+/* Cancels a request still waiting in the queue (RLE_ERR_INVALID_ARG if it
+ * already launched or is unknown); it completes with RLE_ERR_CANCELLED. */
+rle_status rle_server_cancel(rle_server* s, uint64_t ticket);
+/* Waits up to timeout_ms for one request (RLE_ERR_TIMEOUT if it has not
+ * completed); on completion fills *out if given. */
+rle_status rle_server_wait(rle_server* s, uint64_t ticket, int timeout_ms, rle_completion* out);
+/* Waits up to timeout_ms until nothing is queued or running. */
+rle_status rle_server_drain(rle_server* s, int timeout_ms);
+/* Completions not yet taken, oldest first (up to max). */
+rle_status rle_server_poll(rle_server* s, rle_completion* out, int max, int* n);
+rle_status rle_server_get_stats(rle_server* s, rle_server_stats* out);
+/* Clears the latency record and counters (not the queue). */
+rle_status rle_server_reset_stats(rle_server* s);
+/* Test hook: the next `count` batch launches fail on the host as a failed
+ * CUDA launch would; their requests complete with RLE_ERR_CUDA and the
+ * server keeps serving.  No device fault is involved. */
+rle_status rle_server_inject_launch_failures(rle_server* s, int count);
+/* Holds (1) or resumes (0) launching; queued requests wait meanwhile. */
+rle_status rle_server_pause(rle_server* s, int paused);
+rle_status rle_server_destroy(rle_server* s);
+
 /* Camera to screen without any device allocation (no counterpart in the
  * reference).  For callers that may not allocate device memory while they
  * run -- a render loop with a hard frame budget (cudaMalloc can synchronise

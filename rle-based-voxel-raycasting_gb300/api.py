@@ -97,6 +97,31 @@ class BatchTuning(C.Structure):
         return (self.tile_rays, self.lanes_per_ray, self.staging, self.threads_per_block, self.use_graph)
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_frames_per_batch", C.c_int),
+                ("max_inflight", C.c_int), ("raybuf_words", C.c_size_t), ("max_samples", C.c_int), ("plain", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", C.c_int), ("cam", Camera), ("view", ViewParams), ("d_colour", C.c_void_p),
+                ("d_depth", C.c_void_p)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("submit_s", C.c_double), ("launch_s", C.c_double),
+                ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("cancelled", C.c_uint64), ("batches", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("pixels", C.c_double), ("busy_s", C.c_double),
+                ("mrays_per_s", C.c_double), ("device_bytes", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class SceneInfo(C.Structure):
     _fields_ = [("device", C.c_int), ("nummaps", C.c_int), ("sx", C.c_int * RLE_MAX_MIPS),
                 ("sy", C.c_int * RLE_MAX_MIPS), ("sz", C.c_int * RLE_MAX_MIPS),
@@ -145,6 +170,18 @@ def _load() -> C.CDLL:
         "rle_batch_render": (C.c_int, [vp, vp, C.POINTER(FrameRequest), C.c_int, vp]),
         "rle_batch_autotune": (C.c_int, [vp, vp, C.POINTER(FrameRequest), C.c_int, C.c_int, C.POINTER(BatchTuning),
                                          C.POINTER(C.c_float)]),
+        "rle_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "rle_server_add_scene": (C.c_int, [vp, vp, C.POINTER(C.c_int)]),
+        "rle_server_submit": (C.c_int, [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+        "rle_server_cancel": (C.c_int, [vp, C.c_uint64]),
+        "rle_server_wait": (C.c_int, [vp, C.c_uint64, C.c_int, C.POINTER(Completion)]),
+        "rle_server_drain": (C.c_int, [vp, C.c_int]),
+        "rle_server_poll": (C.c_int, [vp, C.POINTER(Completion), C.c_int, C.POINTER(C.c_int)]),
+        "rle_server_get_stats": (C.c_int, [vp, C.POINTER(ServerStats)]),
+        "rle_server_reset_stats": (C.c_int, [vp]),
+        "rle_server_inject_launch_failures": (C.c_int, [vp, C.c_int]),
+        "rle_server_pause": (C.c_int, [vp, C.c_int]),
+        "rle_server_destroy": (C.c_int, [vp]),
         "rle_render_frame_noalloc_limit": (C.c_size_t, []),
         "rle_render_frame_noalloc": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, vp, vp]),
     }
@@ -403,6 +440,80 @@ class Batch:
         try:
             if self._h:
                 _lib.rle_batch_free(self._h)
+        except Exception:
+            pass
+
+
+class Server:
+    """Render server (rle_server_*): resident scenes, a request queue and a
+    scheduler thread doing continuous batching (or, with plain=True, one
+    launch per request)."""
+
+    def __init__(self, hbm_budget_bytes: int, raybuf_words: int, max_frames_per_batch: int = 64,
+                 max_inflight: int = 2, max_samples: int = 1920, plain: bool = False, device: int = 0):
+        cfg = ServerConfig(device, hbm_budget_bytes, max_frames_per_batch, max_inflight, raybuf_words, max_samples,
+                           int(plain))
+        h = C.c_void_p()
+        _check(_lib.rle_server_create(C.byref(cfg), C.byref(h)), "rle_server_create")
+        self._h = h
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise RLEError(-1, "Server", "server was destroyed")
+        return self._h
+
+    def add_scene(self, scene: Scene) -> int:
+        sid = C.c_int()
+        _check(_lib.rle_server_add_scene(self.handle, scene.handle, C.byref(sid)), "rle_server_add_scene")
+        return sid.value
+
+    def submit(self, scene_id: int, cam: Camera, view: ViewParams, colour, depth) -> int:
+        r = Request(scene_id, cam, view, ptr(colour), ptr(depth))
+        t = C.c_uint64()
+        _check(_lib.rle_server_submit(self.handle, C.byref(r), C.byref(t)), "rle_server_submit")
+        return t.value
+
+    def cancel(self, ticket: int) -> int:
+        return _lib.rle_server_cancel(self.handle, ticket)
+
+    def wait(self, ticket: int, timeout_ms: int = 10000) -> Completion:
+        c = Completion()
+        _check(_lib.rle_server_wait(self.handle, ticket, timeout_ms, C.byref(c)), "rle_server_wait")
+        return c
+
+    def drain(self, timeout_ms: int = 60000) -> None:
+        _check(_lib.rle_server_drain(self.handle, timeout_ms), "rle_server_drain")
+
+    def poll(self, max_n: int = 4096) -> list:
+        arr = (Completion * max_n)()
+        n = C.c_int()
+        _check(_lib.rle_server_poll(self.handle, arr, max_n, C.byref(n)), "rle_server_poll")
+        return [arr[i] for i in range(n.value)]
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(_lib.rle_server_get_stats(self.handle, C.byref(s)), "rle_server_get_stats")
+        return s
+
+    def reset_stats(self) -> None:
+        _check(_lib.rle_server_reset_stats(self.handle), "rle_server_reset_stats")
+
+    def inject_launch_failures(self, count: int) -> None:
+        _check(_lib.rle_server_inject_launch_failures(self.handle, count), "rle_server_inject_launch_failures")
+
+    def pause(self, paused: bool = True) -> None:
+        _check(_lib.rle_server_pause(self.handle, int(paused)), "rle_server_pause")
+
+    def destroy(self) -> None:
+        if self._h:
+            _check(_lib.rle_server_destroy(self._h), "rle_server_destroy")
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.rle_server_destroy(self._h)
         except Exception:
             pass
 

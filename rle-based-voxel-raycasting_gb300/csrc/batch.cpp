@@ -112,8 +112,8 @@ rle_status prepare_grid(rle_batch* b) {
 }
 
 // Fills the staging block `h` for these frames; returns the frame count.
-rle_status stage_frames(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
-                        unsigned char* h) {
+rle_status stage_frames(rle_batch* b, const rle_scene* scene, const rle_scene* const* scenes,
+                        const rle_frame_request* frames, int n, unsigned char* h) {
     const Layout& L = b->layout;
     auto* hdr = reinterpret_cast<rle::BatchHeader*>(h + L.header);
     auto* ray_start = reinterpret_cast<int*>(h + L.ray_start);
@@ -137,7 +137,12 @@ rle_status stage_frames(rle_batch* b, const rle_scene* scene, const rle_frame_re
                            b->max_samples);
             return RLE_ERR_CAPACITY;
         }
-        st = rle::fill_ray_params(scene, &rm, &rp[i]);
+        const rle_scene* sc = scenes ? scenes[i] : scene;
+        if (!sc || sc->device != b->device) {
+            rle::set_error("rle_batch_render: frame %d: scene missing or on another device", i);
+            return RLE_ERR_INVALID_ARG;
+        }
+        st = rle::fill_ray_params(sc, &rm, &rp[i]);
         if (st != RLE_OK) return st;
         st = rle::fill_resolve_params(&rm, &sp[i]);
         if (st != RLE_OK) return st;
@@ -200,14 +205,14 @@ rle_status enqueue(rle_batch* b, int parity, cudaStream_t s) {
     return rle::launch_resolve_batch(rs, s);
 }
 
-rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
-                         cudaStream_t stream) {
+rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* const* scenes,
+                         const rle_frame_request* frames, int n, cudaStream_t stream) {
     const int par = b->parity;
     if (b->staged_used[par]) {
         const cudaError_t e = cudaEventSynchronize(b->staged[par]);
         if (e != cudaSuccess) return cuda_fail(e, "rle_batch_render: waiting for the staging block");
     }
-    rle_status st = stage_frames(b, scene, frames, n, b->h_params[par]);
+    rle_status st = stage_frames(b, scene, scenes, frames, n, b->h_params[par]);
     if (st != RLE_OK) return st;
     if (!b->raycast_blocks) {
         st = prepare_grid(b);
@@ -358,8 +363,27 @@ extern "C" rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, con
     if (n == 0) return RLE_OK;
     std::lock_guard<std::mutex> lock(b->mu);
     DeviceScope ds(b->device);
-    return render_locked(b, scene, frames, n, static_cast<cudaStream_t>(stream));
+    return render_locked(b, scene, nullptr, frames, n, static_cast<cudaStream_t>(stream));
 }
+
+namespace rle {
+
+rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, const rle_frame_request* frames, int n,
+                               void* stream) {
+    if (!b || !scenes || (n > 0 && !frames) || n < 0 || n > b->max_frames) {
+        set_error("rle_batch_render: batch, scenes and 0..max_frames frames required");
+        return RLE_ERR_INVALID_ARG;
+    }
+    if (n == 0) return RLE_OK;
+    std::lock_guard<std::mutex> lock(b->mu);
+    DeviceScope ds(b->device);
+    return render_locked(b, nullptr, scenes, frames, n, static_cast<cudaStream_t>(stream));
+}
+
+size_t batch_capacity_words(const rle_batch* b) { return b ? b->raybuf_words : 0; }
+int batch_max_frames(const rle_batch* b) { return b ? b->max_frames : 0; }
+
+}  // namespace rle
 
 extern "C" rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames,
                                          int n, int repeats, rle_batch_tuning* best, float* best_ms) {

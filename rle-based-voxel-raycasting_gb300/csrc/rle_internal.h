@@ -139,6 +139,12 @@ struct BatchResolve {
 rle_status launch_raycast_batch(const BatchRaycast& b, void* stream);
 rle_status launch_resolve_batch(const BatchResolve& b, void* stream);
 int resolve_batch_blocks(int width, int height);  // 256-pixel blocks of one frame
+
+// A batch whose frames may come from different scenes (one per frame).
+rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, const rle_frame_request* frames, int n,
+                               void* stream);
+size_t batch_capacity_words(const rle_batch* b);
+int batch_max_frames(const rle_batch* b);
 rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks);
 
 }  // namespace rle

@@ -1,0 +1,153 @@
+"""Render server (rle_server_*): continuous batching over resident scenes.
+
+- every result served in a mixed stream equals the same request rendered
+  alone (bit for bit), for the batching and the plain server;
+- admission: budgets and per-request limits refuse cleanly;
+- failure handling without any device fault: cancelled requests, bounded
+  waits that time out, and injected launch failures (host side) that fail
+  only their own batch while the server keeps serving.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RES = [(256, 256), (640, 480), (320, 240), (400, 300)]
+
+
+@pytest.fixture(scope="module")
+def scenes(rle, torch_cuda):
+    out = []
+    for n, seed in ((256, 3), (128, 4)):
+        data = rle.scenegen_rle4(rle.scenegen_default(n, 256, n, seed, caves=True))
+        out.append(rle.Scene.from_bytes(data))
+    yield out
+    for s in out:
+        s.free()
+
+
+def _requests(rle, scenes, n, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        sid = int(rng.integers(0, len(scenes)))
+        sc = scenes[sid]
+        info = sc.info()
+        table, words = sc.copy_level(0)
+        x, z = rng.uniform(0, info.sx[0], 2)
+        g = rle.ground_height(table, words, info.sx[0], info.sy[0], int(x), int(z))
+        cam = rle.camera(float(x), float(z), g + float(rng.uniform(10, 60)), float(rng.uniform(0, 360)),
+                         float(rng.uniform(2, 40) * rng.choice([-1, 1])))
+        w, h = RES[i % len(RES)]
+        reqs.append((sid, cam, rle.view_params(w, h, mip_distance=64)))
+    return reqs
+
+
+def _buffers(torch, reqs):
+    return [(torch.full((v.width * v.height,), 5, dtype=torch.int32, device="cuda"),
+             torch.full((v.width * v.height,), 5.0, dtype=torch.float32, device="cuda")) for _, _, v in reqs]
+
+
+def _alone(rle, torch, scene, cam, view):
+    n = view.width * view.height
+    ws_bytes = rle.frame_workspace_bytes(view)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    c = torch.empty(n, dtype=torch.int32, device="cuda")
+    d = torch.empty(n, dtype=torch.float32, device="cuda")
+    rle.render_frame(scene, cam, view, ws, ws_bytes, c, d)
+    torch.cuda.synchronize()
+    return c.cpu().numpy().view(np.uint32), d.cpu().numpy()
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_served_results_equal_alone(rle, scenes, torch_cuda, plain):
+    torch = torch_cuda
+    srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
+                     max_samples=640, plain=plain)
+    ids = [srv.add_scene(s) for s in scenes]
+    assert ids == [0, 1]
+    reqs = _requests(rle, scenes, 24, 7)
+    bufs = _buffers(torch, reqs)
+    tickets = []
+    for (sid, cam, view), (c, d) in zip(reqs, bufs):
+        tickets.append(srv.submit(sid, cam, view, c, d))
+    for t in tickets:
+        assert srv.wait(t, 20000).status == 0
+    srv.drain(20000)
+    torch.cuda.synchronize()
+    for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
+        wc, wd = _alone(rle, torch, scenes[sid], cam, view)
+        assert np.array_equal(c.cpu().numpy().view(np.uint32), wc), f"request {i} colour"
+        assert np.array_equal(d.cpu().numpy().view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+    st = srv.stats()
+    assert st.completed == 24 and st.failed == 0
+    assert st.p99_ms >= st.p50_ms > 0 and st.mrays_per_s > 0
+    if plain:
+        assert st.batches == 24
+    else:
+        assert st.batches < 24  # requests were batched
+    done = srv.poll()
+    assert sorted(c.ticket for c in done) == sorted(tickets)
+    srv.destroy()
+
+
+def test_admission_limits(rle, scenes, torch_cuda):
+    torch = torch_cuda
+    with pytest.raises(rle.RLEError) as e:
+        rle.Server(hbm_budget_bytes=1 << 20, raybuf_words=8 << 20)  # ray buffers alone exceed 1 MiB
+    assert e.value.name == "RLE_ERR_NO_MEMORY"
+    srv = rle.Server(hbm_budget_bytes=(200 << 20), raybuf_words=4 << 20, max_frames_per_batch=4, max_inflight=2,
+                     max_samples=640)
+    srv.add_scene(scenes[1])
+    big = rle.Scene.from_bytes(rle.scenegen_rle4(rle.scenegen_default(1024, 256, 1024, 5)))
+    with pytest.raises(rle.RLEError) as e:
+        srv.add_scene(big)  # would exceed the budget
+    assert e.value.name == "RLE_ERR_NO_MEMORY"
+    big.free()
+    cam = rle.camera(10.5, 10.5, 200.0, 0.0, -20.0)
+    c = torch.empty(1920 * 1080, dtype=torch.int32, device="cuda")
+    d = torch.empty(1920 * 1080, dtype=torch.float32, device="cuda")
+    with pytest.raises(rle.RLEError) as e:
+        srv.submit(0, cam, rle.view_params(1920, 1080), c, d)  # 1920 samples > max_samples 640
+    assert e.value.name == "RLE_ERR_CAPACITY"
+    with pytest.raises(rle.RLEError):
+        srv.submit(7, cam, rle.view_params(320, 240), c, d)  # unknown scene
+    srv.destroy()
+
+
+def test_cancel_timeout_and_injected_failures(rle, scenes, torch_cuda):
+    torch = torch_cuda
+    srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=4, max_inflight=2,
+                     max_samples=640)
+    srv.add_scene(scenes[0])
+    reqs = [(0, cam, view) for _, cam, view in _requests(rle, scenes[:1], 10, 11)]
+    bufs = _buffers(torch, reqs)
+    srv.pause(True)
+    tickets = [srv.submit(sid, cam, view, c, d) for (sid, cam, view), (c, d) in zip(reqs, bufs)]
+    # nothing launches while paused: a bounded wait gives up
+    with pytest.raises(rle.RLEError) as e:
+        srv.wait(tickets[0], 30)
+    assert e.value.name == "RLE_ERR_TIMEOUT"
+    with pytest.raises(rle.RLEError) as e:
+        srv.drain(10)
+    assert e.value.name == "RLE_ERR_TIMEOUT"
+    # queued requests can be cancelled
+    assert srv.cancel(tickets[1]) == 0
+    assert srv.cancel(tickets[1]) != 0  # not twice
+    assert srv.wait(tickets[1], 100).status == -8  # RLE_ERR_CANCELLED
+    # the first launch fails on the host; the rest are served
+    srv.inject_launch_failures(1)
+    srv.pause(False)
+    statuses = [srv.wait(t, 20000).status for t in tickets]
+    st = srv.stats()
+    assert statuses[1] == -8
+    failed = [s for s in statuses if s == -4]  # RLE_ERR_CUDA
+    assert 1 <= len(failed) <= 4  # exactly the first batch
+    assert statuses.count(0) == 10 - 1 - len(failed)
+    assert st.failed == len(failed) and st.cancelled == 1
+    # the server still works afterwards
+    t = srv.submit(0, reqs[0][1], reqs[0][2], bufs[0][0], bufs[0][1])
+    assert srv.wait(t, 20000).status == 0
+    srv.destroy()
