@@ -98,14 +98,21 @@ def test_admission_limits(rle, scenes, torch_cuda):
     with pytest.raises(rle.RLEError) as e:
         rle.Server(hbm_budget_bytes=1 << 20, raybuf_words=8 << 20)  # ray buffers alone exceed 1 MiB
     assert e.value.name == "RLE_ERR_NO_MEMORY"
-    srv = rle.Server(hbm_budget_bytes=(200 << 20), raybuf_words=4 << 20, max_frames_per_batch=4, max_inflight=2,
-                     max_samples=640)
+    probe = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=4 << 20, max_frames_per_batch=4, max_inflight=2,
+                       max_samples=640)
+    buffers = probe.stats().device_bytes
+    probe.destroy()
+    small = scenes[1].info().device_bytes
+    big = rle.Scene.from_bytes(rle.scenegen_rle4(rle.scenegen_default(512, 256, 512, 5)))
+    big_bytes = big.info().device_bytes
+    assert big_bytes > 1024
+    srv = rle.Server(hbm_budget_bytes=buffers + small + big_bytes - 1, raybuf_words=4 << 20, max_frames_per_batch=4,
+                     max_inflight=2, max_samples=640)
     srv.add_scene(scenes[1])
-    big = rle.Scene.from_bytes(rle.scenegen_rle4(rle.scenegen_default(1024, 256, 1024, 5)))
     with pytest.raises(rle.RLEError) as e:
-        srv.add_scene(big)  # would exceed the budget
+        srv.add_scene(big)  # one byte over the budget
     assert e.value.name == "RLE_ERR_NO_MEMORY"
-    big.free()
+    assert srv.stats().device_bytes == buffers + small
     cam = rle.camera(10.5, 10.5, 200.0, 0.0, -20.0)
     c = torch.empty(1920 * 1080, dtype=torch.int32, device="cuda")
     d = torch.empty(1920 * 1080, dtype=torch.float32, device="cuda")
@@ -115,6 +122,13 @@ def test_admission_limits(rle, scenes, torch_cuda):
     with pytest.raises(rle.RLEError):
         srv.submit(7, cam, rle.view_params(320, 240), c, d)  # unknown scene
     srv.destroy()
+    # exactly at the budget the scene is admitted
+    srv = rle.Server(hbm_budget_bytes=buffers + small + big_bytes, raybuf_words=4 << 20, max_frames_per_batch=4,
+                     max_inflight=2, max_samples=640)
+    srv.add_scene(scenes[1])
+    assert srv.add_scene(big) == 1
+    srv.destroy()
+    big.free()
 
 
 def test_cancel_timeout_and_injected_failures(rle, scenes, torch_cuda):
