@@ -377,8 +377,9 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
     seeds 3-6), Poisson arrivals at `lam` requests/s for `seconds`, each
     request a uniform scene and a resolution from SERVE_RES, seeded poses
     (config-2 law), HBM budget 120 GB.  Served twice -- continuous batching
-    and one launch per request -- at the same offered load, then both at
-    saturation (every request queued at once)."""
+    and one launch per request -- at the same offered load, at twice that
+    load (the same requests, arrival times halved), then at saturation
+    (every request queued at once)."""
     if scenes is None:
         scenes = []
         for n, s in SERVE_SCENES:
@@ -416,12 +417,13 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
             srv.wait(srv.submit(sid, cam, v, outs[k][0], outs[k][1]))
         srv.reset_stats()
         entry = {}
-        for load in ("offered", "saturated"):
+        for load in ("offered", "offered_2x", "saturated"):
             srv.reset_stats()
             t0 = time.perf_counter()
+            rate = {"offered": 1.0, "offered_2x": 2.0}.get(load)
             for i, (sid, cam, v) in enumerate(reqs):
-                if load == "offered":
-                    delay = t0 + arrivals[i] - time.perf_counter()
+                if rate:
+                    delay = t0 + arrivals[i] / rate - time.perf_counter()
                     if delay > 0:
                         time.sleep(delay)
                 c, d = outs[i % ring]

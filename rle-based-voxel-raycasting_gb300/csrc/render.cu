@@ -742,13 +742,22 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
     uint32_t* mask_words = smem + L.slot * max_words;
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
-    const int grab = tile * staging;  // staging depth: tiles a group claims at once
+    // Guided self-scheduling: a group claims up to tile * staging rays, but
+    // never more than half its fair share of what is left, so the last rays
+    // go out one at a time and no group is left with a long private tail.
+    const int grab = tile * staging;
+    const int groups = static_cast<int>(gridDim.x) * (static_cast<int>(blockDim.x) / G);
     for (;;) {
-        unsigned int t0 = 0;
-        if (L.k == 0) t0 = atomicAdd(&hdr->next_ray, static_cast<unsigned int>(grab));
+        unsigned int t0 = 0, n = 1;
+        if (L.k == 0) {
+            const int seen = static_cast<int>(*reinterpret_cast<volatile unsigned int*>(&hdr->next_ray));
+            n = static_cast<unsigned int>(max(1, min(grab, (total - seen) / (2 * groups))));
+            t0 = atomicAdd(&hdr->next_ray, n);
+        }
         t0 = __shfl_sync(L.gmask, t0, lane_base(L.gmask));
+        n = __shfl_sync(L.gmask, n, lane_base(L.gmask));
         if (static_cast<int>(t0) >= total) break;
-        const int t1 = min(static_cast<int>(t0) + grab, total);
+        const int t1 = min(static_cast<int>(t0) + static_cast<int>(n), total);
         for (int r = static_cast<int>(t0); r < t1; r++) {
             if (r < ray_start[f] || r >= ray_start[f + 1]) {
                 int lo = 0, hi = nframes - 1;  // last frame with ray_start <= r
