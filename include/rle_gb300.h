@@ -115,6 +115,37 @@ rle_status rle_scenegen_dense(const rle_scenegen_params* p, int mip, uint8_t* bi
 void rle_host_free(void* p);
 
 /* ---------------------------------------------------------------------- */
+/* Scene building on the GPU                                              */
+/* ---------------------------------------------------------------------- */
+/* Both calls build a device-resident scene with kernels only: mip levels,
+ * surface extraction, run-length encoding and the column tables are
+ * computed in device memory and nothing passes through the host.  A level
+ * may hold up to 2^32 - 1 slab words (the .rle4 file stores a signed 32-bit
+ * count, src/Rle4.cpp:279,297).  They block until the scene is ready and
+ * use temporary device memory of about 2 x the level-0 bit volume plus
+ * 16 bytes per level-0 column.  The result is freed with rle_scene_free. */
+
+/* The generator of rle_scenegen_rle4 run on the GPU.  The scene equals,
+ * bit for bit, rle_scenegen_rle4 + rle_scene_load_memory for the same
+ * parameters (tables, slab words, statistics).
+ * Replaces RLE4::compress_all (src/Rle4.cpp:14-48) -> Tree::get_mipmap
+ * (src/tree.h:23-85) -> RLE4::compress (src/Rle4.cpp:52-198) ->
+ * RLE4::all_to_gpu (src/Rle4.cpp:432-448) for generated scenes. */
+rle_status rle_scenegen_device(const rle_scenegen_params* p, int device, rle_scene** out);
+
+/* RLE4::compress_all for a caller's voxel volume already on the device:
+ * d_bits is level 0 in the reference's Tree layout (bit i&7 of byte
+ * (i + j*sx + k*sx*sy) >> 3, j = 0 the top of the column), sx and sz powers
+ * of two >= 8, 1 <= sy <= 1024.  Levels 1..nummaps-1 are Tree::get_mipmap's
+ * >= 3-of-8 rule.  Colour word of a stored voxel (i, j, k) of level m:
+ * d_colours[(i<<m) + (j<<m)*sx + (k<<m)*sx*sy] when d_colours is not NULL
+ * (u16 per level-0 voxel, same index as the bits), else the reference's
+ * normal-derived word without material bits (src/Rle4.cpp:134-161, col1 ==
+ * NULL).  Reads the inputs on `device`; does not modify them. */
+rle_status rle_encode_device(const uint8_t* d_bits, const uint16_t* d_colours, int sx, int sy, int sz,
+                             int nummaps, int device, rle_scene** out);
+
+/* ---------------------------------------------------------------------- */
 /* Cameras and ray maps                                                   */
 /* ---------------------------------------------------------------------- */
 

@@ -154,6 +154,8 @@ def _load() -> C.CDLL:
         "rle_scenegen_rle4": (C.c_int, [C.POINTER(ScenegenParams), C.POINTER(vp), C.POINTER(C.c_size_t)]),
         "rle_scenegen_dense": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, vp, vp]),
         "rle_host_free": (None, [vp]),
+        "rle_scenegen_device": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, C.POINTER(vp)]),
+        "rle_encode_device": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
         "rle_raymap_build": (C.c_int, [C.POINTER(Camera), C.POINTER(ViewParams), C.POINTER(RayMap)]),
         "rle_raybuf_words": (C.c_size_t, [C.POINTER(RayMap)]),
         "rle_tuning_set": (C.c_int, [C.POINTER(Tuning)]),
@@ -256,6 +258,25 @@ class Scene:
 
     def __init__(self, handle: C.c_void_p):
         self._h = handle
+
+    @classmethod
+    def generate_on_device(cls, params: ScenegenParams, device: int = 0) -> "Scene":
+        """rle_scenegen_device: the seeded generator, mips and encoder run as
+        kernels straight into device memory (same scene as from_bytes of
+        scenegen_rle4(params))."""
+        h = C.c_void_p()
+        _check(_lib.rle_scenegen_device(C.byref(params), device, C.byref(h)), "rle_scenegen_device")
+        return cls(h)
+
+    @classmethod
+    def encode_on_device(cls, bits, colours, sx: int, sy: int, sz: int, nummaps: int = 4,
+                         device: int = 0) -> "Scene":
+        """rle_encode_device: RLE4::compress_all of a device bit volume in the
+        reference's Tree layout (optional u16 colour per voxel, same index)."""
+        h = C.c_void_p()
+        _check(_lib.rle_encode_device(ptr(bits), ptr(colours), sx, sy, sz, nummaps, device, C.byref(h)),
+               "rle_encode_device")
+        return cls(h)
 
     @classmethod
     def from_file(cls, path: str, device: int = 0) -> "Scene":

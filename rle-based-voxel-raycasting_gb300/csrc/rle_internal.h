@@ -3,6 +3,8 @@
 
 #include <vector_types.h>
 
+#include "scenegen_math.h"
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -146,5 +148,10 @@ rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, con
 size_t batch_capacity_words(const rle_batch* b);
 int batch_max_frames(const rle_batch* b);
 rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks);
+
+// Scene generator pieces shared by the host and device generators.
+rle_status scenegen_check(const rle_scenegen_params* p);
+void scenegen_perm(uint64_t seed, uint8_t* perm512);
+gen::Consts scenegen_consts(const rle_scenegen_params& p);
 
 }  // namespace rle

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "rle_internal.h"
+#include "scenegen_math.h"
 
 namespace {
 
@@ -32,133 +33,74 @@ inline uint64_t splitmix64(uint64_t& s) {
     return z ^ (z >> 31);
 }
 
-inline uint32_t hash32(uint32_t a, uint32_t b, uint32_t c, uint32_t seed) {
-    uint32_t h = seed ^ 0x9E3779B9u;
-    h ^= a * 0x85EBCA6Bu; h = (h << 13) | (h >> 19); h *= 0xC2B2AE35u;
-    h ^= b * 0x27D4EB2Fu; h = (h << 11) | (h >> 21); h *= 0x165667B1u;
-    h ^= c * 0x9E3779B1u; h = (h << 7) | (h >> 25); h *= 0x85EBCA6Bu;
-    h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
-    return h;
+}  // namespace
+
+namespace rle {
+
+// The generator's permutation table: 0..255 shuffled by a splitmix64
+// Fisher-Yates pass, repeated twice.
+void scenegen_perm(uint64_t seed, uint8_t* perm) {
+    uint8_t p[256];
+    for (int i = 0; i < 256; i++) p[i] = static_cast<uint8_t>(i);
+    uint64_t s = seed ^ 0x5DEECE66Dull;
+    for (int i = 255; i > 0; i--) {
+        const int j = static_cast<int>(splitmix64(s) % static_cast<uint64_t>(i + 1));
+        const uint8_t t = p[i];
+        p[i] = p[j];
+        p[j] = t;
+    }
+    for (int i = 0; i < 512; i++) perm[i] = p[i & 255];
 }
 
-inline int ifloor(float v) {
-    int i = static_cast<int>(v);
-    return (v < static_cast<float>(i)) ? i - 1 : i;
+gen::Consts scenegen_consts(const rle_scenegen_params& q) {
+    gen::Consts c;
+    c.sx = q.sx;
+    c.sy = q.sy;
+    c.sz = q.sz;
+    c.octaves = q.octaves;
+    c.base_period = q.base_period;
+    c.caves = q.caves;
+    c.height_min = q.height_min;
+    c.height_max = q.height_max;
+    c.cave_y0 = q.cave_y0;
+    c.cave_y1 = q.cave_y1;
+    c.cave_threshold = q.cave_threshold;
+    c.cave_period = q.cave_period;
+    c.seed32 = static_cast<uint32_t>(q.seed ^ (q.seed >> 32));
+    return c;
 }
 
-// Value noise on a periodic lattice (period lx x lz cells of `cell` voxels).
-float value_noise2(int x, int z, int cell, int lx, int lz, uint32_t seed) {
-    const int ix = x / cell, iz = z / cell;
-    const float fx = static_cast<float>(x - ix * cell) / static_cast<float>(cell);
-    const float fz = static_cast<float>(z - iz * cell) / static_cast<float>(cell);
-    const int x0 = ix % lx, z0 = iz % lz, x1 = (ix + 1) % lx, z1 = (iz + 1) % lz;
-    const float inv = 1.0f / 16777216.0f;
-    const float v00 = static_cast<float>(hash32(x0, z0, cell, seed) >> 8) * inv;
-    const float v10 = static_cast<float>(hash32(x1, z0, cell, seed) >> 8) * inv;
-    const float v01 = static_cast<float>(hash32(x0, z1, cell, seed) >> 8) * inv;
-    const float v11 = static_cast<float>(hash32(x1, z1, cell, seed) >> 8) * inv;
-    const float sx = fx * fx * (3.0f - 2.0f * fx);
-    const float sz = fz * fz * (3.0f - 2.0f * fz);
-    const float a = v00 + (v10 - v00) * sx;
-    const float b = v01 + (v11 - v01) * sx;
-    return a + (b - a) * sz;
+rle_status scenegen_check(const rle_scenegen_params* p) {
+    if (!p) return RLE_ERR_INVALID_ARG;
+    auto pow2 = [](int v) { return v >= 8 && (v & (v - 1)) == 0; };
+    if (!pow2(p->sx) || !pow2(p->sz) || p->sx > 65536 || p->sz > 65536 || p->sy < 64 || p->sy > 1024 ||
+        (p->sy & 63) != 0 || p->nummaps < 1 || p->nummaps > RLE_MAX_MIPS || p->octaves < 1 ||
+        p->base_period < 1 || (p->base_period & (p->base_period - 1)) != 0 || p->base_period > p->sx ||
+        p->base_period > p->sz || !(p->height_max >= p->height_min) || !(p->cave_period > 0.0f)) {
+        rle::set_error("rle_scenegen: invalid parameters (sx/sz powers of two >= 8, sy multiple of 64 <= 1024, "
+                       "base_period a power of two <= sx, sz)");
+        return RLE_ERR_INVALID_ARG;
+    }
+    if ((p->sx >> (p->nummaps - 1)) < 1 || (p->sz >> (p->nummaps - 1)) < 1 || (p->sy >> (p->nummaps - 1)) < 1) {
+        rle::set_error("rle_scenegen: too many mip levels for the grid");
+        return RLE_ERR_INVALID_ARG;
+    }
+    return RLE_OK;
 }
 
-struct Simplex3 {
-    uint8_t perm[512];
-    explicit Simplex3(uint64_t seed) {
-        uint8_t p[256];
-        for (int i = 0; i < 256; i++) p[i] = static_cast<uint8_t>(i);
-        uint64_t s = seed ^ 0x5DEECE66Dull;
-        for (int i = 255; i > 0; i--) {
-            const int j = static_cast<int>(splitmix64(s) % static_cast<uint64_t>(i + 1));
-            const uint8_t t = p[i];
-            p[i] = p[j];
-            p[j] = t;
-        }
-        for (int i = 0; i < 512; i++) perm[i] = p[i & 255];
-    }
-    static float grad_dot(int h, float x, float y, float z) {
-        // the 12 edge directions of a cube
-        static const signed char g[12][3] = {{1, 1, 0}, {-1, 1, 0}, {1, -1, 0}, {-1, -1, 0},
-                                             {1, 0, 1}, {-1, 0, 1}, {1, 0, -1}, {-1, 0, -1},
-                                             {0, 1, 1}, {0, -1, 1}, {0, 1, -1}, {0, -1, -1}};
-        const signed char* d = g[h % 12];
-        return static_cast<float>(d[0]) * x + static_cast<float>(d[1]) * y + static_cast<float>(d[2]) * z;
-    }
-    float operator()(float x, float y, float z) const {
-        const float F = 1.0f / 3.0f, G = 1.0f / 6.0f;
-        const float s = (x + y + z) * F;
-        const int i = ifloor(x + s), j = ifloor(y + s), k = ifloor(z + s);
-        const float t = static_cast<float>(i + j + k) * G;
-        const float x0 = x - (static_cast<float>(i) - t);
-        const float y0 = y - (static_cast<float>(j) - t);
-        const float z0 = z - (static_cast<float>(k) - t);
-        int i1, j1, k1, i2, j2, k2;
-        if (x0 >= y0) {
-            if (y0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
-            else if (x0 >= z0) { i1 = 1; j1 = 0; k1 = 0; i2 = 1; j2 = 0; k2 = 1; }
-            else { i1 = 0; j1 = 0; k1 = 1; i2 = 1; j2 = 0; k2 = 1; }
-        } else {
-            if (y0 < z0) { i1 = 0; j1 = 0; k1 = 1; i2 = 0; j2 = 1; k2 = 1; }
-            else if (x0 < z0) { i1 = 0; j1 = 1; k1 = 0; i2 = 0; j2 = 1; k2 = 1; }
-            else { i1 = 0; j1 = 1; k1 = 0; i2 = 1; j2 = 1; k2 = 0; }
-        }
-        const float xs[4] = {x0, x0 - static_cast<float>(i1) + G, x0 - static_cast<float>(i2) + 2.0f * G, x0 - 1.0f + 3.0f * G};
-        const float ys[4] = {y0, y0 - static_cast<float>(j1) + G, y0 - static_cast<float>(j2) + 2.0f * G, y0 - 1.0f + 3.0f * G};
-        const float zs[4] = {z0, z0 - static_cast<float>(k1) + G, z0 - static_cast<float>(k2) + 2.0f * G, z0 - 1.0f + 3.0f * G};
-        const int ii = i & 255, jj = j & 255, kk = k & 255;
-        const int hs[4] = {perm[ii + perm[jj + perm[kk]]],
-                           perm[ii + i1 + perm[jj + j1 + perm[kk + k1]]],
-                           perm[ii + i2 + perm[jj + j2 + perm[kk + k2]]],
-                           perm[ii + 1 + perm[jj + 1 + perm[kk + 1]]]};
-        float n = 0.0f;
-        for (int c = 0; c < 4; c++) {
-            float w = 0.6f - xs[c] * xs[c] - ys[c] * ys[c] - zs[c] * zs[c];
-            if (w > 0.0f) {
-                w *= w;
-                n += w * w * grad_dot(hs[c], xs[c], ys[c], zs[c]);
-            }
-        }
-        return 32.0f * n;
-    }
-};
+}  // namespace rle
+
+namespace {
+
+rle_status check_params(const rle_scenegen_params* p) { return rle::scenegen_check(p); }
 
 struct Gen {
-    rle_scenegen_params p;
-    uint32_t seed32;
-    Simplex3 simplex;
+    rle::gen::Consts c;
+    uint8_t perm[512];
     int words;  // u64 words per column at level 0
 
-    explicit Gen(const rle_scenegen_params& q)
-        : p(q), seed32(static_cast<uint32_t>(q.seed ^ (q.seed >> 32))), simplex(q.seed), words(q.sy / 64) {}
-
-    int ground_height(int x, int z) const {
-        float sum = 0.0f, amp = 1.0f, norm = 0.0f;
-        int cell = p.base_period;
-        for (int o = 0; o < p.octaves && cell >= 1; o++) {
-            sum += amp * value_noise2(x, z, cell, p.sx / cell, p.sz / cell, seed32 + 101u * static_cast<uint32_t>(o));
-            norm += amp;
-            amp *= 0.5f;
-            cell >>= 1;
-        }
-        const float f = sum / norm;
-        // stretch the fBm's central concentration over the height range
-        float g = (f - 0.5f) * 1.8f + 0.5f;
-        if (g < 0.0f) g = 0.0f;
-        if (g > 1.0f) g = 1.0f;
-        int h = static_cast<int>(p.height_min + (p.height_max - p.height_min) * g);
-        if (h < 1) h = 1;
-        if (h > p.sy) h = p.sy;
-        return h;
-    }
-
-    bool carved(int x, int y, int z) const {
-        const float inv = 1.0f / p.cave_period;
-        const float fx = static_cast<float>(x) * inv, fy = static_cast<float>(y) * inv * 4.0f,
-                    fz = static_cast<float>(z) * inv;
-        const float d = simplex(fx, fy, fz) + 0.5f * simplex(2.0f * fx + 17.0f, 2.0f * fy, 2.0f * fz + 31.0f);
-        return d > p.cave_threshold;
+    explicit Gen(const rle_scenegen_params& q) : c(rle::scenegen_consts(q)), words(q.sy / 64) {
+        rle::scenegen_perm(q.seed, perm);
     }
 
     // Level-0 solid bits of column (x, z): u64 words, bit j of word j/64.
@@ -167,41 +109,24 @@ struct Gen {
     // edge by that sign), so storage index j is sy-1 minus the height y.
     void column(int x, int z, uint64_t* out) const {
         std::memset(out, 0, sizeof(uint64_t) * words);
-        const int h = ground_height(x, z);
+        const int h = rle::gen::ground_height(c, x, z);
         for (int y = 0; y < h; y++) {
-            const int j = p.sy - 1 - y;
+            const int j = c.sy - 1 - y;
             out[j >> 6] |= 1ull << (j & 63);
         }
-        if (p.caves) {
-            int y0 = static_cast<int>(p.cave_y0), y1 = static_cast<int>(p.cave_y1);
+        if (c.caves) {
+            int y0 = static_cast<int>(c.cave_y0), y1 = static_cast<int>(c.cave_y1);
             if (y0 < 1) y0 = 1;
             if (y1 > h) y1 = h;
             for (int y = y0; y < y1; y++) {
-                const int j = p.sy - 1 - y;
-                if (carved(x, y, z)) out[j >> 6] &= ~(1ull << (j & 63));
+                const int j = c.sy - 1 - y;
+                if (rle::gen::carved(c, perm, x, y, z)) out[j >> 6] &= ~(1ull << (j & 63));
             }
         }
     }
 
     // RGB565 colour of level-0 voxel (x, j, z), j counted down from the top.
-    uint16_t colour(int x, int j, int z) const {
-        const int y = p.sy - 1 - j;
-        static const uint8_t pal[8][3] = {{92, 78, 66},   {150, 130, 90},  {196, 180, 120}, {96, 150, 70},
-                                          {70, 124, 58},  {118, 112, 100}, {150, 146, 140}, {236, 236, 240}};
-        int band = y * 8 / p.sy;
-        if (band > 7) band = 7;
-        if (band < 0) band = 0;
-        const int cell = 64 < p.sx && 64 < p.sz ? 64 : (p.sx < p.sz ? p.sx : p.sz);
-        const int tint = static_cast<int>(value_noise2(x & (p.sx - 1), z & (p.sz - 1), cell, p.sx / cell,
-                                                       p.sz / cell, seed32 ^ 0xC0105EEDu) * 96.0f);
-        const int jitter = static_cast<int>(hash32(x, y, z, seed32) & 31);
-        const int f = 176 + tint + jitter;  // 176..303, /256
-        int r = pal[band][0] * f >> 8, g = pal[band][1] * f >> 8, b = pal[band][2] * f >> 8;
-        if (r > 255) r = 255;
-        if (g > 255) g = 255;
-        if (b > 255) b = 255;
-        return static_cast<uint16_t>(((r >> 3) << 11) | ((g >> 2) << 5) | (b >> 3));
-    }
+    uint16_t colour(int x, int j, int z) const { return rle::gen::colour(c, rle::gen::tint(c, x, z), x, j, z); }
 };
 
 // One level as column bitsets: cols[(z*sx + x) * words + w].
@@ -331,26 +256,7 @@ int encode_column(const uint64_t* surf, int sy, const Gen& g, int x, int z, int 
     return 2 + n_head + n_col;
 }
 
-rle_status check_params(const rle_scenegen_params* p) {
-    if (!p) return RLE_ERR_INVALID_ARG;
-    auto pow2 = [](int v) { return v >= 8 && (v & (v - 1)) == 0; };
-    if (!pow2(p->sx) || !pow2(p->sz) || p->sx > 65536 || p->sz > 65536 || p->sy < 64 || p->sy > 1024 ||
-        (p->sy & 63) != 0 || p->nummaps < 1 || p->nummaps > RLE_MAX_MIPS || p->octaves < 1 ||
-        p->base_period < 1 || (p->base_period & (p->base_period - 1)) != 0 || p->base_period > p->sx ||
-        p->base_period > p->sz || !(p->height_max >= p->height_min) || !(p->cave_period > 0.0f)) {
-        rle::set_error("rle_scenegen: invalid parameters (sx/sz powers of two >= 8, sy multiple of 64 <= 1024, "
-                       "base_period a power of two <= sx, sz)");
-        return RLE_ERR_INVALID_ARG;
-    }
-    if ((p->sx >> (p->nummaps - 1)) < 1 || (p->sz >> (p->nummaps - 1)) < 1 || (p->sy >> (p->nummaps - 1)) < 1) {
-        rle::set_error("rle_scenegen: too many mip levels for the grid");
-        return RLE_ERR_INVALID_ARG;
-    }
-    return RLE_OK;
-}
-
-void build_levels(const Gen& g, std::vector<BitLevel>& lv) {
-    const rle_scenegen_params& p = g.p;
+void build_levels(const rle_scenegen_params& p, const Gen& g, std::vector<BitLevel>& lv) {
     lv.resize(p.nummaps);
     BitLevel& L0 = lv[0];
     L0.sx = p.sx;
@@ -399,7 +305,7 @@ extern "C" rle_status rle_scenegen_rle4(const rle_scenegen_params* p, void** byt
     try {
         const Gen g(*p);
         std::vector<BitLevel> lv;
-        build_levels(g, lv);
+        build_levels(*p, g, lv);
         // pass 1: words per column; pass 2: fill
         std::vector<std::vector<uint64_t>> starts(p->nummaps);
         size_t total = 4;
@@ -465,7 +371,7 @@ extern "C" rle_status rle_scenegen_dense(const rle_scenegen_params* p, int mip, 
     try {
         const Gen g(*p);
         std::vector<BitLevel> lv;
-        build_levels(g, lv);
+        build_levels(*p, g, lv);
         const BitLevel& L = lv[mip];
         const size_t sxy = static_cast<size_t>(L.sx) * L.sy;
         if (bits) std::memset(bits, 0, (static_cast<size_t>(L.sx) * L.sy * L.sz + 7) / 8);

@@ -116,6 +116,13 @@ def test_invalid_arguments_return_status(rle):
     h = C.c_void_p()
     assert lib.rle_scene_load_memory(b"\x01\x00", 2, 0, C.byref(h)) == -3  # truncated header
     assert lib.rle_scene_load_file(b"/nonexistent.rle4", 0, C.byref(h)) == -2
+    # device scene builders validate before any device work
+    assert lib.rle_scenegen_device(C.byref(p), 0, C.byref(h)) == -1
+    assert lib.rle_encode_device(None, None, 64, 64, 64, 4, 0, C.byref(h)) == -1  # no bits
+    fake = C.c_void_p(16)  # never dereferenced: the sizes are refused first
+    assert lib.rle_encode_device(fake, None, 48, 64, 64, 4, 0, C.byref(h)) == -1  # sx not a power of two
+    assert lib.rle_encode_device(fake, None, 64, 2048, 64, 4, 0, C.byref(h)) == -1  # sy > 1024
+    assert lib.rle_encode_device(fake, None, 8, 64, 64, 5, 0, C.byref(h)) == -1  # 8 >> 4 == 0
 
 
 def test_malformed_rle4_rejected_before_upload(rle, po):
