@@ -248,6 +248,9 @@ def run_ours(args):
     serving = None
     if args.serve_seconds > 0:
         serving = run_serving(rle, torch, seconds=args.serve_seconds)
+    config5 = None
+    if args.config5_frames > 0:
+        config5 = run_config5(rle, torch, frames=args.config5_frames)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -293,6 +296,8 @@ def run_ours(args):
         line["batched_vs_plain"] = batched
     if serving:
         line["serving"] = serving
+    if config5:
+        line["config5_8192"] = config5
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -368,6 +373,87 @@ def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
     }
 
 
+def run_config5(rle, torch, frames=120, views_per_batch=8, seed=7, repeats=3):
+    """Config 5: the 8192^2 x 512 cave scene (seed 7) built on the GPU
+    (generator, mips, encoder and column tables as kernels), then 3840x2160
+    frames at 75 deg FOV with LOD switches at 256/512/1024 (mip_distance 256),
+    poses 20-200 voxels above the ground, rendered plain (one launch pair per
+    frame) and batched (8 views per launch)."""
+    p = rle.scenegen_default(8192, 512, 8192, seed, caves=True)
+    builds = []
+    scene = None
+    for _ in range(repeats):
+        if scene is not None:
+            scene.free()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        scene = rle.Scene.generate_on_device(p)
+        builds.append(time.perf_counter() - t0)
+    info = scene.info()
+    table, words = scene.copy_level(0)
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(frames):
+        x, z = rng.uniform(0, 8192, 2)
+        g = rle.ground_height(table, words, 8192, 512, int(x), int(z))
+        cams.append(rle.camera(float(x), float(z), g + float(rng.uniform(20, 200)), float(rng.uniform(0, 360)),
+                               float(rng.uniform(1, 30) * rng.choice([-1, 1])), 75.0, scene_height=512))
+    W4, H4 = 3840, 2160
+    view = rle.view_params(W4, H4, mip_distance=256)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    outs = [(torch.empty(W4 * H4, dtype=torch.int32, device="cuda"),
+             torch.empty(W4 * H4, dtype=torch.float32, device="cuda")) for _ in range(views_per_batch)]
+    ws_bytes = rle.frame_workspace_bytes(view)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+
+    def plain():
+        for i, cam in enumerate(cams):
+            c, d = outs[i % views_per_batch]
+            rle.render_frame(scene, cam, view, ws, ws_bytes, c, d, None, stream=sp)
+
+    groups = [[rle.frame_request(cam, view, *outs[k]) for k, cam in enumerate(cams[i:i + views_per_batch])]
+              for i in range(0, frames, views_per_batch)]
+    batch = rle.Batch(max_frames=views_per_batch, raybuf_words=max(rle.batch_words_needed(g) for g in groups),
+                      max_samples=4096)
+
+    def batched():
+        for g in groups:
+            batch.render(scene, g, stream=sp)
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    plain_ms = timed(plain)
+    batch_ms = timed(batched)
+    batch.free()
+    del ws
+    pixels = W4 * H4 * frames
+    slab_bytes = sum(int(info.slab_words[m]) * 2 for m in range(info.nummaps))
+    out = {
+        "workload": f"config 5: 8192x8192x512 cave scene seed 7 built on the GPU; {frames} frames 3840x2160, "
+                    f"75 deg FOV, mip switches 256/512/1024, poses 20-200 above ground",
+        "scene_build_s": round(float(np.median(builds)), 4),
+        "scene_device_bytes": int(info.device_bytes),
+        "slab_bytes": slab_bytes,
+        "runs_per_column": round(info.run_headers / (8192 * 8192), 2),
+        "plain": {"value": round(pixels / plain_ms / 1e3, 1), "unit": "Mrays/s", "ms_per_frame": round(plain_ms / frames, 4)},
+        "batched": {"value": round(pixels / batch_ms / 1e3, 1), "unit": "Mrays/s",
+                    "ms_per_frame": round(batch_ms / frames, 4), "views_per_launch": views_per_batch},
+    }
+    scene.free()
+    return out
+
+
 SERVE_RES = [((256, 256), 0.4), ((640, 480), 0.3), ((1280, 720), 0.2), ((1920, 1080), 0.1)]
 SERVE_SCENES = [(1024, 3), (2048, 4), (2048, 5), (4096, 6)]
 
@@ -383,7 +469,7 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
     if scenes is None:
         scenes = []
         for n, s in SERVE_SCENES:
-            scenes.append(rle.Scene.from_bytes(rle.scenegen_rle4(rle.scenegen_default(n, 256, n, s, caves=True))))
+            scenes.append(rle.Scene.generate_on_device(rle.scenegen_default(n, 256, n, s, caves=True)))
     rng = np.random.default_rng(seed)
     levels = []
     for sc in scenes:
@@ -518,6 +604,8 @@ def main(argv=None):
     ap.add_argument("--cpu-frames", type=int, default=3, help="frames in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the config-3 batched-vs-plain comparison")
+    ap.add_argument("--config5-frames", type=int, default=120,
+                    help="4K frames of the config-5 run on the 8192^2 x 512 scene (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
                     help="seconds of Poisson arrivals in the config-4 serving comparison (0: skip)")
     args = ap.parse_args(argv)

@@ -224,14 +224,23 @@ struct Cell {
     int mip;
     int vx, vz;
     bool loaded;
+    int nrec;  // candidate runs recorded by prepare_cell; -1: too many, walk the runs
 };
 
-template <int G>
-__device__ __forceinline__ void draw_run(const RayParams& P, const Ray& R, const Mask& mask, unsigned gmask,
-                                         int k, uint32_t* row, float* drow, rle_hit* hrow, const uint16_t* colours,
-                                         int y, int scr_y2, float sgs, float sgf, float tex, int texture,
-                                         float pz, float py, int mip, int vx, int vz, Counts& cnt, bool count) {
-    const float res_y2 = static_cast<float>(P.S / 2);
+// Candidate runs a lane records per cell for the merge (shared memory,
+// 3 x float4 per run).
+constexpr int kRecs = 4;
+
+// Per-span constants of the perspective-correct fill (:642-700): screen
+// position of the span's far end, texture and 1/z gradients along the span.
+struct Span {
+    float scr_y1r, u1z, u2dz, onez1, onedz2, umax;
+    int texture, sg0;
+};
+
+__device__ __forceinline__ Span span_setup(float res_y2, const Ray& R, float pz, float py, float sgs, float sgf,
+                                           float tex, int texture) {
+    Span sp;
     const float pz1r = pz + R.pos3d_z_add * sgs;
     const float py1r = py + R.pos3d_y_add * sgs;
     const float pz2r = pz + R.pos3d_z_add * sgf;
@@ -244,12 +253,29 @@ __device__ __forceinline__ void draw_run(const RayParams& P, const Ray& R, const
     float onedz2 = 1 / pz1r - onez1;
     u2dz /= scr_y2r - scr_y1r;
     onedz2 /= scr_y2r - scr_y1r;
+    sp.scr_y1r = scr_y1r;
+    sp.u1z = u1z;
+    sp.u2dz = u2dz;
+    sp.onez1 = onez1;
+    sp.onedz2 = onedz2;
+    sp.umax = static_cast<float>(static_cast<double>(tex) - 1.0);
+    sp.texture = texture;
+    sp.sg0 = static_cast<int>(sgs);
+    return sp;
+}
+
+// Fills samples y .. scr_y2-1 of a span that the occupancy mask leaves open.
+template <int G>
+__device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int k, uint32_t* row, float* drow,
+                                          rle_hit* hrow, const uint16_t* colours, int y, int scr_y2, const Span& sp,
+                                          int mip, int vx, int vz, Counts& cnt, bool count) {
+    const float u2dz = sp.u2dz, onedz2 = sp.onedz2;
     if (count) cnt.spans++;
-    const float mult = static_cast<float>(y + 1) - scr_y1r;
-    float uz = u1z + u2dz * mult;
-    float onez = onez1 + onedz2 * mult;
-    const float umin = static_cast<float>(texture);
-    const float umax = static_cast<float>(static_cast<double>(tex) - 1.0);
+    const float mult = static_cast<float>(y + 1) - sp.scr_y1r;
+    float uz = sp.u1z + u2dz * mult;
+    float onez = sp.onez1 + onedz2 * mult;
+    const float umin = static_cast<float>(sp.texture);
+    const float umax = sp.umax;
     // G pixels per pass: the accumulation runs in lockstep in every lane (it
     // is a chain of IEEE additions, one per sample, masked or not); lane k
     // keeps the values of sample y + k and does its divisions in parallel.
@@ -278,7 +304,7 @@ __device__ __forceinline__ void draw_run(const RayParams& P, const Ray& R, const
                 rle_hit h;
                 h.x = static_cast<uint16_t>(vx);
                 h.z = static_cast<uint16_t>(vz);
-                h.y = static_cast<uint16_t>((static_cast<int>(sgs) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
+                h.y = static_cast<uint16_t>((sp.sg0 >> mip) + static_cast<int>(u - static_cast<uint32_t>(sp.texture)));
                 h.mip = static_cast<uint8_t>(mip);
                 h.flags = 1;
                 hrow[yy] = h;
@@ -355,8 +381,8 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
         }
         const int y = mask.first_clear(scr_y1, scr_y2);
         if (y >= scr_y2) continue;
-        draw_run<G>(P, R, mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sgs, sgf, tex, texture,
-                           c.pz, c.py, c.mip, c.vx, c.vz, cnt, count);
+        const Span sp = span_setup(res_y2, R, c.pz, c.py, sgs, sgf, tex, texture);
+        draw_span<G>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, c.mip, c.vx, c.vz, cnt, count);
     }
 }
 
@@ -424,8 +450,20 @@ __device__ __forceinline__ void lod_switch(Walk& w, int nummaps) {
 // Derives the cell of one DDA step, pre-culls it against the horizon at the
 // start of the chunk, fetches its column-table entry and scans its runs.
 // Returns whether the exact walk could draw from it.
+//
+// The scan also records, in `rec` (this lane's kRecs slots), every run the
+// exact walk could still draw, with its projection and span constants, so
+// that the sequential merge needs no per-run arithmetic.  A run is recorded
+// unless, at the chunk's horizon, the walk would skip it for good (`pz1 <= 0`,
+// `pz2 <= 0`, `scr_y1 >= ymax`); the walk's break test (`scr_y2 <= ymin`) of
+// the skipped runs before a recorded run is folded into that run's guard (the
+// smallest scr_y2 among them and its own), since nothing changes between
+// those tests.  The scan ends where the walk would already break at the
+// chunk's horizon.  More than kRecs such runs: c.nrec = -1, and the merge
+// walks the runs itself.
 __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, bool valid, float before, float delta,
-                                             float pbx, float pby, int ib, int mip, int ymin, int ymax, Cell& c) {
+                                             float pbx, float pby, int ib, int mip, int ymin, int ymax, Cell& c,
+                                             float4* rec) {
     const float res_y2 = static_cast<float>(P.S / 2);
     const float sin_x = P.sin_x, cos_x = P.cos_x;
     const float mountain = P.posy;
@@ -448,6 +486,7 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
     c.cyy = cyy * R.rmul;
     c.ex = 0;
     c.ey = 0;
+    c.nrec = 0;
     // clip top at the chunk's horizon; for pz >= 0 it only gets truer as ymin grows
     const bool culled = c.pz >= 0.0f && c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin);
     c.loaded = valid && !culled;
@@ -455,17 +494,19 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
     const uint2 e = __ldg(&P.table[mip][static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip)]);
     c.ex = e.x;
     c.ey = e.y;
-    // any run that could still draw at the chunk's horizon?  (runs culled
-    // here are culled by the exact walk too: ymin only grows, ymax only shrinks)
     const uint16_t* hdr = P.slabs[mip] + 2 + c.ex;
     const int nruns = c.ey & 0xffffu;
+    const uint32_t colour_ofs = c.ex + 2u + static_cast<uint32_t>(nruns);
     uint32_t sti = c.ey >> 16;
-    int sg = 0;
+    int sg = 0, texi = 0, n = 0;
+    int guard = 0x7fffffff;
     for (int r = 0; r < nruns; r++) {
         if (r > 0) sti = __ldg(&hdr[r]);
         int solid = static_cast<int>(sti >> 10);
         sg += static_cast<int>(sti & 1023u) << mip;
         if (solid == 0) continue;
+        const int texture = texi;
+        texi += solid;
         solid <<= mip;
         const float sgs = static_cast<float>(sg);
         sg += solid;
@@ -476,7 +517,8 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
         if (pz1 <= 0) continue;
         const float py1 = cyy1 + R.pos3d_y_add * sgs;
         const int scr_y2 = static_cast<int>(res_y2 + py1 / pz1);
-        if (scr_y2 <= ymin) return false;
+        if (scr_y2 <= ymin) break;  // the walk breaks here or earlier
+        guard = min(guard, scr_y2);
         float czz2 = c.pz, cyy2 = c.py;
         if (mountain + sgf < 0) { czz2 += c.czz; cyy2 += c.cyy; }
         const float pz2 = czz2 + R.pos3d_z_add * sgf;
@@ -484,9 +526,63 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
         const float py2 = cyy2 + R.pos3d_y_add * sgf;
         const int scr_y1 = static_cast<int>(res_y2 + py2 / pz2 - 1);
         if (scr_y1 >= ymax) continue;
-        return true;
+        if (n == kRecs) {
+            n = -1;
+            break;
+        }
+        // tex counts colours in float in the walk; integers this small are exact
+        const Span sp = span_setup(res_y2, R, c.pz, c.py, sgs, sgf, static_cast<float>(texi), texture);
+        rec[3 * n + 0] = make_float4(__int_as_float(guard), __int_as_float(scr_y2), __int_as_float(scr_y1),
+                                     __uint_as_float(colour_ofs));
+        rec[3 * n + 1] = make_float4(sp.scr_y1r, sp.u1z, sp.u2dz, sp.onez1);
+        rec[3 * n + 2] = make_float4(sp.onedz2, sp.umax, __int_as_float(sp.texture), __int_as_float(sp.sg0));
+        guard = 0x7fffffff;
+        n++;
     }
-    return false;
+    c.nrec = n;
+    return n != 0;
+}
+
+// The exact walk over the runs prepare_cell recorded for one cell (same
+// tests, same order, same horizon updates as merge_cell).
+template <int G>
+__device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& mask, unsigned gmask, int k,
+                                               uint32_t* row, float* drow, rle_hit* hrow, const float4* rec, int nrec,
+                                               float pz, float py, int mip, int vx, int vz, int& ymin, int& ymax,
+                                               Counts& cnt) {
+    const float res_y2 = static_cast<float>(P.S / 2);
+    // clip top (:467)
+    if (pz * res_y2 + py <= pz * static_cast<float>(ymin)) return;
+    for (int r = 0; r < nrec; r++) {
+        const float4 a = rec[3 * r];
+        if (__float_as_int(a.x) <= ymin) break;
+        int scr_y2 = __float_as_int(a.y), scr_y1 = __float_as_int(a.z);
+        if (scr_y1 >= ymax) continue;
+        // floating horizon (:563-580)
+        if (scr_y2 >= ymax) {
+            scr_y2 = ymax;
+            ymax = scr_y1;
+        }
+        if (scr_y1 <= ymin) {
+            scr_y1 = ymin;
+            ymin = scr_y2;
+            ymin = mask.first_clear(ymin, ymax > ymin ? ymax : ymin);
+        }
+        const int y = mask.first_clear(scr_y1, scr_y2);
+        if (y >= scr_y2) continue;
+        const float4 b = rec[3 * r + 1], d = rec[3 * r + 2];
+        Span sp;
+        sp.scr_y1r = b.x;
+        sp.u1z = b.y;
+        sp.u2dz = b.z;
+        sp.onez1 = b.w;
+        sp.onedz2 = d.x;
+        sp.umax = d.y;
+        sp.texture = __float_as_int(d.z);
+        sp.sg0 = __float_as_int(d.w);
+        const uint16_t* colours = P.slabs[mip] + __float_as_uint(a.w);
+        draw_span<G>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, mip, vx, vz, cnt, false);
+    }
 }
 
 // Whether no cell at or beyond DDA distance t0 can draw a span.
@@ -523,14 +619,15 @@ __device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, fl
 // active = false: the lanes only take part in the group's collectives.
 // chunks of G DDA steps, lane k taking step k of each.
 template <int G>
-__device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, int k,
-                                         unsigned gmask, Counts& cnt) {
+__device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, float4* recs,
+                                         int k, unsigned gmask, Counts& cnt) {
     const int S = P.S;
     const int words = (S + 31) >> 5;
     const bool hits = P.rayhit != nullptr;
     const bool count = P.counters != nullptr;
     Mask mask{mask_words};
 
+    float4* my_recs = recs + static_cast<size_t>(threadIdx.x) * (3 * kRecs);
     Ray R;
     Walk W;
     bool live = false;
@@ -636,10 +733,12 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
 
             // ---- 2. each lane: its cell -- pre-cull, fetch, run scan ----
             Cell c;
-            const bool drawable = prepare_cell(P, R, valid, before, delta, pbx, pby, ib, smip, ymin, ymax, c);
+            const bool drawable =
+                prepare_cell(P, R, valid, before, delta, pbx, pby, ib, smip, ymin, ymax, c, my_recs);
             // with counters every valid cell goes through the exact walk
             unsigned todo = __ballot_sync(gmask, count ? valid : drawable) >> lane_base(gmask);
             if (G < 32) todo &= (1u << G) - 1u;
+            __syncwarp(gmask);  // the records are read by the whole group
 
             // ---- 3. exact sequential merge of the cells that may draw ----
             bool stop = false;
@@ -647,17 +746,15 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                 const int s = __ffs(todo) - 1;
                 todo &= todo - 1;
                 const int src = lane_base(gmask) + s;
-                Cell cs;
-                cs.pz = __shfl_sync(gmask, c.pz, src);
-                cs.py = __shfl_sync(gmask, c.py, src);
-                cs.czz = __shfl_sync(gmask, c.czz, src);
-                cs.cyy = __shfl_sync(gmask, c.cyy, src);
-                cs.ex = __shfl_sync(gmask, c.ex, src);
-                cs.ey = __shfl_sync(gmask, c.ey, src);
-                cs.mip = __shfl_sync(gmask, c.mip, src);
-                cs.vx = __shfl_sync(gmask, c.vx, src);
-                cs.vz = __shfl_sync(gmask, c.vz, src);
-                cs.loaded = __shfl_sync(gmask, static_cast<int>(c.loaded), src) != 0;
+                const float pz = __shfl_sync(gmask, c.pz, src);
+                const float py = __shfl_sync(gmask, c.py, src);
+                const int packed = __shfl_sync(gmask, (c.nrec + 1) | (c.mip << 8), src);
+                const int nrec = (packed & 0xff) - 1, mip = packed >> 8;
+                int vx = 0, vz = 0;
+                if (hits) {
+                    vx = __shfl_sync(gmask, c.vx, src);
+                    vz = __shfl_sync(gmask, c.vz, src);
+                }
                 // the reference ends the ray when its horizon closes, checked
                 // at every step before the cell (:370)
                 if (ymin >= ymax) {
@@ -665,8 +762,26 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                     break;
                 }
                 if (count) cnt.cells++;  // with counters every valid step is visited
-                merge_cell<G>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, cnt, count);
+                if (count || nrec < 0) {
+                    Cell cs;
+                    cs.pz = pz;
+                    cs.py = py;
+                    cs.czz = __shfl_sync(gmask, c.czz, src);
+                    cs.cyy = __shfl_sync(gmask, c.cyy, src);
+                    cs.ex = __shfl_sync(gmask, c.ex, src);
+                    cs.ey = __shfl_sync(gmask, c.ey, src);
+                    cs.mip = mip;
+                    cs.vx = __shfl_sync(gmask, c.vx, src);
+                    cs.vz = __shfl_sync(gmask, c.vz, src);
+                    cs.loaded = __shfl_sync(gmask, static_cast<int>(c.loaded), src) != 0;
+                    merge_cell<G>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, cnt, count);
+                } else {
+                    const float4* rec = recs + static_cast<size_t>((threadIdx.x & ~31u) + src) * (3 * kRecs);
+                    merge_recorded<G>(P, mask, gmask, k, row, drow, hrow, rec, nrec, pz, py, mip, vx, vz, ymin, ymax,
+                                      cnt);
+                }
             }
+            __syncwarp(gmask);  // records are rewritten by the next chunk
             if (stop || ymin >= ymax || ended) break;
             // Nothing further along this ray can be drawn once every run of
             // every later cell projects below the floating horizon (the
@@ -700,6 +815,16 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
     cnt = Counts();
 }
 
+// Shared memory of a raycast block: the rays' occupancy masks (`words` per
+// ray slot), then, 16-byte aligned, kRecs run records per thread.
+__host__ __device__ __forceinline__ int mask_region_words(int slots, int words) {
+    return (slots * words + 3) & ~3;
+}
+__host__ __device__ __forceinline__ size_t raycast_smem_bytes(int threads, int slots, int words) {
+    return static_cast<size_t>(mask_region_words(slots, words)) * 4 +
+           static_cast<size_t>(threads) * kRecs * 3 * sizeof(float4);
+}
+
 // Lane layout of a group of G lanes within a block.
 template <int G>
 struct Lanes {
@@ -723,8 +848,9 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
     const int rays_per_block = (blockDim.x >> 5) * (32 / G);
     const int x = blockIdx.x * rays_per_block + L.slot;
     const int words = (P.S + 31) >> 5;
+    float4* recs = reinterpret_cast<float4*>(smem + mask_region_words(rays_per_block, words));
     Counts cnt;
-    cast_ray<G>(P, x, x < P.rays, smem + L.slot * words, L.k, L.gmask, cnt);
+    cast_ray<G>(P, x, x < P.rays, smem + L.slot * words, recs, L.k, L.gmask, cnt);
 }
 
 // Many frames in one persistent launch.  The rays of all frames form one
@@ -740,6 +866,8 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
     const int nframes = hdr->nframes;
     const int total = ray_start[nframes];
     uint32_t* mask_words = smem + L.slot * max_words;
+    float4* recs = reinterpret_cast<float4*>(
+        smem + mask_region_words((static_cast<int>(blockDim.x) >> 5) * (32 / G), max_words));
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
     // Guided self-scheduling: a group claims up to tile * staging rays, but
@@ -768,7 +896,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 }
                 f = lo;
             }
-            cast_ray<G>(frames[f], r - ray_start[f], true, mask_words, L.k, L.gmask, cnt);
+            cast_ray<G>(frames[f], r - ray_start[f], true, mask_words, recs, L.k, L.gmask, cnt);
         }
     }
 }
@@ -777,7 +905,7 @@ template <int G>
 rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
     const int words = (p.S + 31) >> 5;
     const int rays_per_block = threads / 32 * (32 / G);
-    const size_t smem = static_cast<size_t>(rays_per_block) * words * 4;
+    const size_t smem = raycast_smem_bytes(threads, rays_per_block, words);
     if (smem > 227 * 1024) {
         set_error("rle_render_rays: %d samples per ray exceed shared memory at this launch shape", p.S);
         return RLE_ERR_CAPACITY;
@@ -800,7 +928,7 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
 
 template <int G>
 size_t batch_smem(int threads, int max_samples) {
-    return static_cast<size_t>(threads / 32 * (32 / G)) * ((max_samples + 31) >> 5) * 4;
+    return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5);
 }
 
 template <int G>
