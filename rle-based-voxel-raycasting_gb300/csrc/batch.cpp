@@ -102,7 +102,7 @@ void release(rle_batch* b) {
 
 rle_status prepare_grid(rle_batch* b) {
     rle_status st = rle::batch_grid_blocks(b->tuning.lanes_per_ray, b->tuning.threads_per_block, b->max_samples,
-                                           &b->raycast_blocks);
+                                           b->with_hits, &b->raycast_blocks);
     if (st != RLE_OK) return st;
     int sms = 0;
     const cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
@@ -195,6 +195,7 @@ rle_status enqueue(rle_batch* b, int parity, cudaStream_t s) {
     rc.threads = b->tuning.threads_per_block;
     rc.max_samples = b->max_samples;
     rc.blocks = b->raycast_blocks;
+    rc.hits = b->with_hits ? 1 : 0;
     rle_status st = rle::launch_raycast_batch(rc, s);
     if (st != RLE_OK) return st;
     rle::BatchResolve rs;

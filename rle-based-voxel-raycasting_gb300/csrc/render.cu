@@ -224,12 +224,26 @@ struct Cell {
     int mip;
     int vx, vz;
     bool loaded;
-    int nrec;  // candidate runs recorded by prepare_cell; -1: too many, walk the runs
+    int nrec;    // candidate runs recorded by scan_runs; -1: too many, walk the runs
+    int guard0;  // guard of the first recorded run (the cell is a no-op once ymin reaches it)
 };
 
 // Candidate runs a lane records per cell for the merge (shared memory,
 // 3 x float4 per run).
 constexpr int kRecs = 4;
+
+// A lane's last coloured sample, stored one pass late: the colour gather
+// (a dependent load) then overlaps the following work instead of stalling
+// the group at the store.  Every sample is written once, so the order of
+// the stores does not matter.
+struct Pending {
+    uint32_t* at = nullptr;
+    uint32_t colour = 0, z = 0;
+    __device__ __forceinline__ void flush() {
+        if (at) *at = colour + z;
+        at = nullptr;
+    }
+};
 
 // Per-span constants of the perspective-correct fill (:642-700): screen
 // position of the span's far end, texture and 1/z gradients along the span.
@@ -265,12 +279,12 @@ __device__ __forceinline__ Span span_setup(float res_y2, const Ray& R, float pz,
 }
 
 // Fills samples y .. scr_y2-1 of a span that the occupancy mask leaves open.
-template <int G>
+template <int G, bool kCount>
 __device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int k, uint32_t* row, float* drow,
                                           rle_hit* hrow, const uint16_t* colours, int y, int scr_y2, const Span& sp,
-                                          int mip, int vx, int vz, Counts& cnt, bool count) {
+                                          int mip, int vx, int vz, Pending& pend, Counts& cnt) {
     const float u2dz = sp.u2dz, onedz2 = sp.onedz2;
-    if (count) cnt.spans++;
+    if constexpr (kCount) cnt.spans++;
     const float mult = static_cast<float>(y + 1) - sp.scr_y1r;
     float uz = sp.u1z + u2dz * mult;
     float onez = sp.onez1 + onedz2 * mult;
@@ -297,8 +311,10 @@ __device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int 
             const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(my_uz / my_onez, umin), umax));
             const float depth = 1 / my_onez;
             const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
-            const uint32_t c16 = __ldg(&colours[u]);
-            row[yy] = c16 + (real_z << 16);
+            pend.flush();
+            pend.at = &row[yy];
+            pend.colour = __ldg(&colours[u]);
+            pend.z = real_z << 16;
             drow[yy] = depth;
             if (hrow) {
                 rle_hit h;
@@ -312,17 +328,17 @@ __device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int 
             atomicOr(&mask.w[yy >> 5], 1u << (yy & 31));
             wrote = true;
         }
-        if (count) cnt.pixels += __popc(__ballot_sync(gmask, wrote));
+        if constexpr (kCount) cnt.pixels += __popc(__ballot_sync(gmask, wrote));
         __syncwarp(gmask);
     }
 }
 
 // Exact sequential processing of one cell (the body of the reference's main
 // loop after the DDA step).  Uniform across the G lanes of the group.
-template <int G>
+template <int G, bool kCount>
 __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, const Mask& mask, unsigned gmask, int k,
                                            uint32_t* row, float* drow, rle_hit* hrow, Cell c, int& ymin, int& ymax,
-                                           Counts& cnt, bool count) {
+                                           Pending& pend, Counts& cnt) {
     const float res_y2 = static_cast<float>(P.S / 2);
     // clip top (:467)
     if (c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin)) return;
@@ -332,7 +348,7 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
         c.ex = e.x;
         c.ey = e.y;
     }
-    if (count) cnt.fetched++;
+    if constexpr (kCount) cnt.fetched++;
     const uint16_t* hdr = P.slabs[c.mip] + 2 + c.ex;
     const int nruns = c.ey & 0xffffu;
     const uint16_t* colours = hdr + nruns;
@@ -343,7 +359,7 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
     for (int r = 0; r < nruns; r++) {
         if (r > 0) {
             sti = __ldg(&hdr[r]);
-            if (count) cnt.headers++;
+            if constexpr (kCount) cnt.headers++;
         }
         int solid = static_cast<int>(sti >> 10);
         sg += static_cast<int>(sti & 1023u) << c.mip;
@@ -354,7 +370,7 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
         const float sgs = static_cast<float>(sg);
         sg += solid;
         const float sgf = static_cast<float>(sg);
-        if (count) cnt.runs++;
+        if constexpr (kCount) cnt.runs++;
         float czz1 = c.pz, cyy1 = c.py;
         if (mountain + sgs >= 0) { czz1 += c.czz; cyy1 += c.cyy; }
         const float pz1 = czz1 + R.pos3d_z_add * sgs;
@@ -382,7 +398,7 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
         const int y = mask.first_clear(scr_y1, scr_y2);
         if (y >= scr_y2) continue;
         const Span sp = span_setup(res_y2, R, c.pz, c.py, sgs, sgf, tex, texture);
-        draw_span<G>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, c.mip, c.vx, c.vz, cnt, count);
+        draw_span<G, kCount>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, c.mip, c.vx, c.vz, pend, cnt);
     }
 }
 
@@ -447,23 +463,11 @@ __device__ __forceinline__ void lod_switch(Walk& w, int nummaps) {
     }
 }
 
-// Derives the cell of one DDA step, pre-culls it against the horizon at the
-// start of the chunk, fetches its column-table entry and scans its runs.
-// Returns whether the exact walk could draw from it.
-//
-// The scan also records, in `rec` (this lane's kRecs slots), every run the
-// exact walk could still draw, with its projection and span constants, so
-// that the sequential merge needs no per-run arithmetic.  A run is recorded
-// unless, at the chunk's horizon, the walk would skip it for good (`pz1 <= 0`,
-// `pz2 <= 0`, `scr_y1 >= ymax`); the walk's break test (`scr_y2 <= ymin`) of
-// the skipped runs before a recorded run is folded into that run's guard (the
-// smallest scr_y2 among them and its own), since nothing changes between
-// those tests.  The scan ends where the walk would already break at the
-// chunk's horizon.  More than kRecs such runs: c.nrec = -1, and the merge
-// walks the runs itself.
-__device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, bool valid, float before, float delta,
-                                             float pbx, float pby, int ib, int mip, int ymin, int ymax, Cell& c,
-                                             float4* rec) {
+// Derives the cell of one DDA step and, unless the horizon known now culls
+// it, starts the fetch of its column-table entry (the value is first used by
+// scan_runs, one chunk later in the pipeline).
+__device__ __forceinline__ void cell_geometry(const RayParams& P, const Ray& R, bool valid, float before, float delta,
+                                              float pbx, float pby, int ib, int mip, int ymin, Cell& c) {
     const float res_y2 = static_cast<float>(P.S / 2);
     const float sin_x = P.sin_x, cos_x = P.cos_x;
     const float mountain = P.posy;
@@ -487,13 +491,40 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
     c.ex = 0;
     c.ey = 0;
     c.nrec = 0;
-    // clip top at the chunk's horizon; for pz >= 0 it only gets truer as ymin grows
+    // clip top at the horizon known now; for pz >= 0 it only gets truer as ymin grows
     const bool culled = c.pz >= 0.0f && c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin);
     c.loaded = valid && !culled;
+    if (c.loaded) {
+        const uint2 e =
+            __ldg(&P.table[mip][static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip)]);
+        c.ex = e.x;
+        c.ey = e.y;
+    }
+}
+
+// Pre-culls a cell against the horizon at the start of its merge and scans
+// its runs.  Returns whether the exact walk could draw from it.
+//
+// The scan also records, in `rec` (this lane's kRecs slots), every run the
+// exact walk could still draw, with its projection and span constants, so
+// that the sequential merge needs no per-run arithmetic.  A run is recorded
+// unless, at the chunk's horizon, the walk would skip it for good (`pz1 <= 0`,
+// `pz2 <= 0`, `scr_y1 >= ymax`); the walk's break test (`scr_y2 <= ymin`) of
+// the skipped runs before a recorded run is folded into that run's guard (the
+// smallest scr_y2 among them and its own), since nothing changes between
+// those tests.  The scan ends where the walk would already break at the
+// chunk's horizon.  More than kRecs such runs: c.nrec = -1, and the merge
+// walks the runs itself.
+__device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int ymin, int ymax, Cell& c,
+                                          float4* rec) {
+    const float res_y2 = static_cast<float>(P.S / 2);
+    const float mountain = P.posy;
+    const int mip = c.mip;
+    c.nrec = 0;
+    c.guard0 = 0x7fffffff;
     if (!c.loaded) return false;
-    const uint2 e = __ldg(&P.table[mip][static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip)]);
-    c.ex = e.x;
-    c.ey = e.y;
+    // clip top at the current horizon
+    if (c.pz >= 0.0f && c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin)) return false;
     const uint16_t* hdr = P.slabs[mip] + 2 + c.ex;
     const int nruns = c.ey & 0xffffu;
     const uint32_t colour_ofs = c.ex + 2u + static_cast<uint32_t>(nruns);
@@ -536,6 +567,7 @@ __device__ __forceinline__ bool prepare_cell(const RayParams& P, const Ray& R, b
                                      __uint_as_float(colour_ofs));
         rec[3 * n + 1] = make_float4(sp.scr_y1r, sp.u1z, sp.u2dz, sp.onez1);
         rec[3 * n + 2] = make_float4(sp.onedz2, sp.umax, __int_as_float(sp.texture), __int_as_float(sp.sg0));
+        if (n == 0) c.guard0 = guard;
         guard = 0x7fffffff;
         n++;
     }
@@ -549,7 +581,7 @@ template <int G>
 __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& mask, unsigned gmask, int k,
                                                uint32_t* row, float* drow, rle_hit* hrow, const float4* rec, int nrec,
                                                float pz, float py, int mip, int vx, int vz, int& ymin, int& ymax,
-                                               Counts& cnt) {
+                                               Pending& pend, Counts& cnt) {
     const float res_y2 = static_cast<float>(P.S / 2);
     // clip top (:467)
     if (pz * res_y2 + py <= pz * static_cast<float>(ymin)) return;
@@ -581,8 +613,89 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
         sp.texture = __float_as_int(d.z);
         sp.sg0 = __float_as_int(d.w);
         const uint16_t* colours = P.slabs[mip] + __float_as_uint(a.w);
-        draw_span<G>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, mip, vx, vz, cnt, false);
+        draw_span<G, false>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, mip, vx, vz, pend, cnt);
     }
+}
+
+// One chunk of the DDA: G steps in lockstep, lane k keeping the state after
+// step k; the state before step k is the state after step k-1 (a shuffle
+// from lane k-1; lane 0 takes the chunk start).  Advances W past the chunk
+// and returns how many of its steps are valid (fewer than G: the ray ends).
+struct ChunkStep {
+    float before, delta, pbx, pby;
+    int ib, mip;
+};
+
+template <int G>
+__device__ __forceinline__ int dda_chunk(const RayParams& P, Walk& W, int k, unsigned gmask, ChunkStep& st) {
+    const float zfar = static_cast<float>(P.z_far);
+    // ---- 1. G DDA steps in lockstep; lane k keeps the state after step k ----
+    // the state before step k is the state after step k-1 (a shuffle
+    // from lane k-1; lane 0 takes the chunk start)
+    const float start_dd = W.d.dd_now, start_px = W.d.pnx, start_py = W.d.pny;
+    const int start_ix = W.d.index;
+    float c_dd = 0, c_px = 0, c_py = 0;
+    int c_ix = 0, smip = W.mip;
+    int nvalid = G;
+    // z, dz and the switch distances are integers held exactly in
+    // floats: when neither a LOD switch nor the end of the ray can
+    // fall inside the chunk, the steps need no checks
+    const int zi = static_cast<int>(W.z), dzi = static_cast<int>(W.dz);
+    const bool plain = W.mapswitch >= zi && (W.mapswitch - zi) / dzi + 1 >= G && (P.z_far - zi) / dzi >= G;
+    if (plain) {
+#pragma unroll
+        for (int s = 0; s < G; s++) {
+            dda_step<G == 32>(W.d);
+            if (s == k) {
+                c_dd = W.d.dd_now;
+                c_px = W.d.pnx;
+                c_py = W.d.pny;
+                c_ix = W.d.index;
+            }
+        }
+        W.z += W.dz * static_cast<float>(G);
+    } else {
+        bool ended_here = false;
+#pragma unroll 1
+        for (int s = 0; s < G; s++) {
+            if (W.z > W.zswitch) {
+                lod_switch(W, P.nummaps);
+                if (k >= s) smip = W.mip;  // cells from step s on use the new level
+            }
+            W.z += W.dz;
+            if (W.z > zfar) {
+                nvalid = s;
+                ended_here = true;
+                break;
+            }
+            dda_step<G == 32>(W.d);
+            if (s == k) {
+                c_dd = W.d.dd_now;
+                c_px = W.d.pnx;
+                c_py = W.d.pny;
+                c_ix = W.d.index;
+            }
+        }
+        (void)ended_here;
+    }
+    float before = __shfl_up_sync(gmask, c_dd, 1);
+    float pbx = __shfl_up_sync(gmask, c_px, 1);
+    float pby = __shfl_up_sync(gmask, c_py, 1);
+    int ib = __shfl_up_sync(gmask, c_ix, 1);
+    if (k == 0) {
+        before = start_dd;
+        pbx = start_px;
+        pby = start_py;
+        ib = start_ix;
+    }
+    const float delta = c_dd - before;
+    st.before = before;
+    st.delta = delta;
+    st.pbx = pbx;
+    st.pby = pby;
+    st.ib = ib;
+    st.mip = smip;
+    return nvalid;
 }
 
 // Whether no cell at or beyond DDA distance t0 can draw a span.
@@ -618,16 +731,15 @@ __device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, fl
 // gmask), using mask_words (S/32 words of shared memory) as its bitmask.
 // active = false: the lanes only take part in the group's collectives.
 // chunks of G DDA steps, lane k taking step k of each.
-template <int G>
+template <int G, bool kCount, bool kHits>
 __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, float4* recs,
                                          int k, unsigned gmask, Counts& cnt) {
     const int S = P.S;
     const int words = (S + 31) >> 5;
-    const bool hits = P.rayhit != nullptr;
-    const bool count = P.counters != nullptr;
     Mask mask{mask_words};
 
     float4* my_recs = recs + static_cast<size_t>(threadIdx.x) * (3 * kRecs);
+    Pending pend;
     Ray R;
     Walk W;
     bool live = false;
@@ -641,11 +753,11 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
     __syncwarp();
     uint32_t* row = active ? P.raybuf + static_cast<size_t>(x) * S : nullptr;
     float* drow = active ? P.raydepth + static_cast<size_t>(x) * S : nullptr;
-    rle_hit* hrow = (hits && active) ? P.rayhit + static_cast<size_t>(x) * S : nullptr;
+    rle_hit* hrow = nullptr;
+    if constexpr (kHits) hrow = (active && P.rayhit) ? P.rayhit + static_cast<size_t>(x) * S : nullptr;
     const int ymin0 = R.ymin, ymax0 = R.ymax;
 
     if (live) {
-        const float zfar = static_cast<float>(P.z_far);
         int ymin = R.ymin, ymax = R.ymax;
         W.mip = 0;
         W.z = 0;
@@ -666,78 +778,31 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                 W.dz *= 2;
             }
         }
+        ChunkStep st;
+        int nvalid = dda_chunk<G>(P, W, k, gmask, st);
+        Cell c;
+        cell_geometry(P, R, k < nvalid, st.before, st.delta, st.pbx, st.pby, st.ib, st.mip, ymin, c);
         for (;;) {
-            // ---- 1. G DDA steps in lockstep; lane k keeps the state after step k ----
-            // the state before step k is the state after step k-1 (a shuffle
-            // from lane k-1; lane 0 takes the chunk start)
-            const float start_dd = W.d.dd_now, start_px = W.d.pnx, start_py = W.d.pny;
-            const int start_ix = W.d.index;
-            float c_dd = 0, c_px = 0, c_py = 0;
-            int c_ix = 0, smip = W.mip;
-            int nvalid = G;
-            // z, dz and the switch distances are integers held exactly in
-            // floats: when neither a LOD switch nor the end of the ray can
-            // fall inside the chunk, the steps need no checks
-            const int zi = static_cast<int>(W.z), dzi = static_cast<int>(W.dz);
-            const bool plain = W.mapswitch >= zi && (W.mapswitch - zi) / dzi + 1 >= G && (P.z_far - zi) / dzi >= G;
-            if (plain) {
-#pragma unroll
-                for (int s = 0; s < G; s++) {
-                    dda_step<G == 32>(W.d);
-                    if (s == k) {
-                        c_dd = W.d.dd_now;
-                        c_px = W.d.pnx;
-                        c_py = W.d.pny;
-                        c_ix = W.d.index;
-                    }
-                }
-                W.z += W.dz * static_cast<float>(G);
-            } else {
-                bool ended_here = false;
-#pragma unroll 1
-                for (int s = 0; s < G; s++) {
-                    if (W.z > W.zswitch) {
-                        lod_switch(W, P.nummaps);
-                        if (k >= s) smip = W.mip;  // cells from step s on use the new level
-                    }
-                    W.z += W.dz;
-                    if (W.z > zfar) {
-                        nvalid = s;
-                        ended_here = true;
-                        break;
-                    }
-                    dda_step<G == 32>(W.d);
-                    if (s == k) {
-                        c_dd = W.d.dd_now;
-                        c_px = W.d.pnx;
-                        c_py = W.d.pny;
-                        c_ix = W.d.index;
-                    }
-                }
-                (void)ended_here;
-            }
             if (nvalid == 0) break;
             const bool ended = nvalid < G;
             const bool valid = k < nvalid;
-            float before = __shfl_up_sync(gmask, c_dd, 1);
-            float pbx = __shfl_up_sync(gmask, c_px, 1);
-            float pby = __shfl_up_sync(gmask, c_py, 1);
-            int ib = __shfl_up_sync(gmask, c_ix, 1);
-            if (k == 0) {
-                before = start_dd;
-                pbx = start_px;
-                pby = start_py;
-                ib = start_ix;
+            const float t_end = W.d.dd_now;  // DDA distance at the end of this chunk
+            // ---- 1. the next chunk's DDA steps and column-table fetches are
+            // issued now; their loads complete while this chunk is merged ----
+            int nvalid_next = 0;
+            Cell c_next;
+            if (!ended) {
+                ChunkStep st_next;
+                nvalid_next = dda_chunk<G>(P, W, k, gmask, st_next);
+                cell_geometry(P, R, k < nvalid_next, st_next.before, st_next.delta, st_next.pbx, st_next.pby,
+                              st_next.ib, st_next.mip, ymin, c_next);
             }
-            const float delta = c_dd - before;
 
-            // ---- 2. each lane: its cell -- pre-cull, fetch, run scan ----
-            Cell c;
-            const bool drawable =
-                prepare_cell(P, R, valid, before, delta, pbx, pby, ib, smip, ymin, ymax, c, my_recs);
+            // ---- 2. each lane: its cell -- pre-cull at the current horizon, run scan ----
+            const bool drawable = scan_runs(P, R, ymin, ymax, c, my_recs);
             // with counters every valid cell goes through the exact walk
-            unsigned todo = __ballot_sync(gmask, count ? valid : drawable) >> lane_base(gmask);
-            if (G < 32) todo &= (1u << G) - 1u;
+            unsigned todo = __ballot_sync(gmask, kCount ? valid : drawable) >> lane_base(gmask);
+            if constexpr (G < 32) todo &= (1u << G) - 1u;
             __syncwarp(gmask);  // the records are read by the whole group
 
             // ---- 3. exact sequential merge of the cells that may draw ----
@@ -751,7 +816,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                 const int packed = __shfl_sync(gmask, (c.nrec + 1) | (c.mip << 8), src);
                 const int nrec = (packed & 0xff) - 1, mip = packed >> 8;
                 int vx = 0, vz = 0;
-                if (hits) {
+                if (kHits && hrow) {
                     vx = __shfl_sync(gmask, c.vx, src);
                     vz = __shfl_sync(gmask, c.vz, src);
                 }
@@ -761,8 +826,8 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                     stop = true;
                     break;
                 }
-                if (count) cnt.cells++;  // with counters every valid step is visited
-                if (count || nrec < 0) {
+                if constexpr (kCount) cnt.cells++;  // with counters every valid step is visited
+                if (kCount || nrec < 0) {
                     Cell cs;
                     cs.pz = pz;
                     cs.py = py;
@@ -774,11 +839,19 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                     cs.vx = __shfl_sync(gmask, c.vx, src);
                     cs.vz = __shfl_sync(gmask, c.vz, src);
                     cs.loaded = __shfl_sync(gmask, static_cast<int>(c.loaded), src) != 0;
-                    merge_cell<G>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, cnt, count);
+                    merge_cell<G, kCount>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, pend, cnt);
                 } else {
                     const float4* rec = recs + static_cast<size_t>((threadIdx.x & ~31u) + src) * (3 * kRecs);
+                    const int ymin_before = ymin;
                     merge_recorded<G>(P, mask, gmask, k, row, drow, hrow, rec, nrec, pz, py, mip, vx, vz, ymin, ymax,
-                                      cnt);
+                                      pend, cnt);
+                    if (ymin != ymin_before) {
+                        // cells whose first recorded run now breaks the walk
+                        // at once are no-ops: drop them all in one vote
+                        unsigned keep = __ballot_sync(gmask, c.nrec < 0 || c.guard0 > ymin) >> lane_base(gmask);
+                        if constexpr (G < 32) keep &= (1u << G) - 1u;
+                        todo &= keep;
+                    }
                 }
             }
             __syncwarp(gmask);  // records are rewritten by the next chunk
@@ -787,9 +860,12 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             // every later cell projects below the floating horizon (the
             // reference walks on to z_far without drawing).  Exact counters
             // need the full walk, so they keep it.
-            if (!count && ray_is_done(P, R, W.d.dd_now, ymin)) break;
+            if (!kCount && ray_is_done(P, R, t_end, ymin)) break;
+            c = c_next;
+            nvalid = nvalid_next;
         }
     }
+    pend.flush();
     __syncwarp();
 
     // ---- coalesced fill of the samples no span coloured ----
@@ -805,7 +881,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             }
         }
     }
-    if (count && active && k == 0) {
+    if (kCount && active && k == 0) {
         // the lanes of a group hold the same counts; lane 0 adds the ray's
         unsigned long long* c = reinterpret_cast<unsigned long long*>(P.counters);
         const unsigned long long v[6] = {cnt.cells, cnt.fetched, cnt.headers, cnt.runs, cnt.spans, cnt.pixels};
@@ -840,8 +916,9 @@ struct Lanes {
     }
 };
 
-// One frame: ray slot s of block b casts ray b * slots + s.
-template <int G>
+// One frame: ray slot s of block b casts ray b * slots + s.  kCount: the
+// DETAIL_BENCH counters (exact walk of every cell); kHits: hit records.
+template <int G, bool kCount, bool kHits>
 __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ RayParams P) {
     extern __shared__ uint32_t smem[];
     const Lanes<G> L;
@@ -850,14 +927,14 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
     const int words = (P.S + 31) >> 5;
     float4* recs = reinterpret_cast<float4*>(smem + mask_region_words(rays_per_block, words));
     Counts cnt;
-    cast_ray<G>(P, x, x < P.rays, smem + L.slot * words, recs, L.k, L.gmask, cnt);
+    cast_ray<G, kCount, kHits>(P, x, x < P.rays, smem + L.slot * words, recs, L.k, L.gmask, cnt);
 }
 
 // Many frames in one persistent launch.  The rays of all frames form one
 // index space (ray_start[f] = first global ray of frame f); each group takes
 // `tile` consecutive rays at a time from a global counter until none are
 // left, so long and short rays of every frame balance across the GPU.
-template <int G>
+template <int G, bool kHits>
 __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, const int* __restrict__ ray_start,
                                                             const RayParams* __restrict__ frames, int tile,
                                                             int staging, int max_words) {
@@ -896,13 +973,13 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 }
                 f = lo;
             }
-            cast_ray<G>(frames[f], r - ray_start[f], true, mask_words, recs, L.k, L.gmask, cnt);
+            cast_ray<G, false, kHits>(frames[f], r - ray_start[f], true, mask_words, recs, L.k, L.gmask, cnt);
         }
     }
 }
 
-template <int G>
-rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
+template <int G, bool kCount, bool kHits>
+rle_status launch_variant(const RayParams& p, int threads, cudaStream_t stream) {
     const int words = (p.S + 31) >> 5;
     const int rays_per_block = threads / 32 * (32 / G);
     const size_t smem = raycast_smem_bytes(threads, rays_per_block, words);
@@ -910,14 +987,14 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
         set_error("rle_render_rays: %d samples per ray exceed shared memory at this launch shape", p.S);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<G, kCount, kHits>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
     }
     const int blocks = (p.rays + rays_per_block - 1) / rays_per_block;
-    raycast_kernel<G><<<blocks, threads, smem, stream>>>(p);
+    raycast_kernel<G, kCount, kHits><<<blocks, threads, smem, stream>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("raycast launch: %s", cudaGetErrorString(e));
@@ -927,24 +1004,34 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
 }
 
 template <int G>
+rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
+    if (p.counters) {
+        return p.rayhit ? launch_variant<G, true, true>(p, threads, stream)
+                        : launch_variant<G, true, false>(p, threads, stream);
+    }
+    return p.rayhit ? launch_variant<G, false, true>(p, threads, stream)
+                    : launch_variant<G, false, false>(p, threads, stream);
+}
+
+template <int G>
 size_t batch_smem(int threads, int max_samples) {
     return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5);
 }
 
-template <int G>
+template <int G, bool kHits>
 rle_status batch_blocks(int threads, int max_samples, int* blocks) {
     const size_t smem = batch_smem<G>(threads, max_samples);
     if (smem > 227 * 1024) {
         set_error("batch: %d samples per ray exceed shared memory at this launch shape", max_samples);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G, kHits>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int dev = 0, sms = 0, per_sm = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G>, threads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G, kHits>, threads, smem);
     if (e != cudaSuccess) {
         set_error("batch launch set-up: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
@@ -953,16 +1040,16 @@ rle_status batch_blocks(int threads, int max_samples, int* blocks) {
     return RLE_OK;
 }
 
-template <int G>
+template <int G, bool kHits>
 rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
     const size_t smem = batch_smem<G>(b.threads, b.max_samples);
     int blocks = b.blocks;
     if (blocks <= 0) {
-        const rle_status st = batch_blocks<G>(b.threads, b.max_samples, &blocks);
+        const rle_status st = batch_blocks<G, kHits>(b.threads, b.max_samples, &blocks);
         if (st != RLE_OK) return st;
     }
-    raycast_batch_kernel<G><<<blocks, b.threads, smem, stream>>>(b.header, b.ray_start, b.frames, b.tile,
-                                                                 b.staging, (b.max_samples + 31) >> 5);
+    raycast_batch_kernel<G, kHits><<<blocks, b.threads, smem, stream>>>(b.header, b.ray_start, b.frames, b.tile,
+                                                                        b.staging, (b.max_samples + 31) >> 5);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("batch raycast launch: %s", cudaGetErrorString(e));
@@ -973,11 +1060,14 @@ rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
 
 }  // namespace
 
-rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks) {
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks) {
     switch (lanes) {
-        case 8: return batch_blocks<8>(threads, max_samples, blocks);
-        case 16: return batch_blocks<16>(threads, max_samples, blocks);
-        case 32: return batch_blocks<32>(threads, max_samples, blocks);
+        case 8: return hits ? batch_blocks<8, true>(threads, max_samples, blocks)
+                            : batch_blocks<8, false>(threads, max_samples, blocks);
+        case 16: return hits ? batch_blocks<16, true>(threads, max_samples, blocks)
+                             : batch_blocks<16, false>(threads, max_samples, blocks);
+        case 32: return hits ? batch_blocks<32, true>(threads, max_samples, blocks)
+                             : batch_blocks<32, false>(threads, max_samples, blocks);
         default:
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;
@@ -991,9 +1081,9 @@ rle_status launch_raycast_batch(const BatchRaycast& b, void* stream) {
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     switch (b.lanes) {
-        case 8: return batch_launch<8>(b, s);
-        case 16: return batch_launch<16>(b, s);
-        case 32: return batch_launch<32>(b, s);
+        case 8: return b.hits ? batch_launch<8, true>(b, s) : batch_launch<8, false>(b, s);
+        case 16: return b.hits ? batch_launch<16, true>(b, s) : batch_launch<16, false>(b, s);
+        case 32: return b.hits ? batch_launch<32, true>(b, s) : batch_launch<32, false>(b, s);
         default:
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;

@@ -131,6 +131,7 @@ struct BatchRaycast {
     int threads;               // block size
     int max_samples;           // largest S of the frames the launch may see
     int blocks;                // grid size (0: fill the GPU)
+    int hits;                  // frames may carry hit buffers
 };
 struct BatchResolve {
     const BatchHeader* header;    // device
@@ -147,7 +148,7 @@ rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, con
                                void* stream);
 size_t batch_capacity_words(const rle_batch* b);
 int batch_max_frames(const rle_batch* b);
-rle_status batch_grid_blocks(int lanes, int threads, int max_samples, int* blocks);
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks);
 
 // Scene generator pieces shared by the host and device generators.
 rle_status scenegen_check(const rle_scenegen_params* p);
