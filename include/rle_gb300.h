@@ -115,6 +115,22 @@ rle_status rle_scenegen_dense(const rle_scenegen_params* p, int mip, uint8_t* bi
 void rle_host_free(void* p);
 
 /* ---------------------------------------------------------------------- */
+/* Soft post-filter                                                       */
+/* ---------------------------------------------------------------------- */
+/* The reference's second display pass, bin/shader/soft.frag, drawn by
+ * src/main.cpp:627-653 over the frame the colorize pass left: per pixel,
+ * a box filter over the neighbours near the front depth (an edge-aware
+ * blur whose radius grows with 1/z).  Input is one resolved frame as
+ * rle_resolve / rle_render_frame write it (RGBA8 colour, float depth; sky
+ * and no-data pixels as documented there); output is RGBA8 (alpha: the
+ * filtered 0.001/z term of the frame buffer).  width, height <= 2048 (the
+ * reference's frame buffer); d_out must not alias d_colour.  Bilinear taps
+ * are computed in single precision and clamp to the frame.  Stream-ordered,
+ * no synchronisation, no allocation. */
+rle_status rle_soft_filter(const uint32_t* d_colour, const float* d_depth, int width, int height,
+                           uint32_t* d_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Scene building on the GPU                                              */
 /* ---------------------------------------------------------------------- */
 /* Both calls build a device-resident scene with kernels only: mip levels,

@@ -95,6 +95,8 @@ def oracle() -> C.CDLL:
         lib.orc_resolve.argtypes = [C.POINTER(OrcRayMap), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.orc_raybuf_rows.argtypes = [C.POINTER(OrcRayMap)]
+        lib.orc_soft_filter.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        lib.orc_soft_filter.restype = None
         lib.orc_rays_to_render.argtypes = [C.POINTER(OrcRayMap)]
         _orc = lib
     return _orc
@@ -248,6 +250,15 @@ def resolve(rm: OrcRayMap, width: int, height: int, raybuf: np.ndarray, raydepth
                          None if fhit is None else fhit.ctypes.data, colour.ctypes.data, depth.ctypes.data,
                          None if hit is None else hit.ctypes.data, None if idx is None else idx.ctypes.data)
     return colour, depth, hit, idx
+
+
+def soft_filter(colour: np.ndarray, depth: np.ndarray, width: int, height: int) -> np.ndarray:
+    """The soft post-filter (bin/shader/soft.frag) of one resolved frame."""
+    c = np.ascontiguousarray(colour, dtype=np.uint32)
+    d = np.ascontiguousarray(depth, dtype=np.float32)
+    out = np.zeros(width * height, np.uint32)
+    oracle().orc_soft_filter(c.ctypes.data, d.ctypes.data, width, height, out.ctypes.data)
+    return out
 
 
 def raymap_from_product(pm) -> OrcRayMap:

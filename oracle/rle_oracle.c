@@ -899,3 +899,123 @@ void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const ui
             }
         }
 }
+
+/* ======================================================================= */
+/* Soft post-filter: bin/shader/soft.frag over the colorize pass's frame    */
+/* buffer (src/main.cpp:627-653; the buffer is RGBA8, GL_LINEAR, clamp to   */
+/* edge, src/GL_Main.h:150-165).                                            */
+/* ======================================================================= */
+
+/* Frame-buffer texel the colorize pass leaves for one resolved pixel: RGB,
+ * and alpha = 0.001/z clamped to [0,1] in 8 bits, z being the sample's
+ * depth16 as the shader reads it (low byte/255/256 + high byte/255); sky
+ * has alpha 0 (colorize_buddha_soft.frag:86-136). */
+static uint32_t soft_texel(const uint32_t* colour, const float* depth, int width, int x, int row)
+{
+    size_t i = (size_t)row * width + x;
+    uint32_t w8;
+    float d = depth[i];
+    if (isinf(d)) {
+        w8 = 0;
+    } else {
+        uint32_t d16 = (uint32_t)(f2i(d) & 0xfffe);
+        float z = ((float)(d16 & 255u) / 255.0f) * (1.0f / 256.0f) + (float)(d16 >> 8) / 255.0f;
+        float fragz = 0.001f / z;
+        float f = fminf(fmaxf(fragz, 0.0f), 1.0f);
+        w8 = (uint32_t)f2i(f * 255.0f + 0.5f);
+    }
+    return (colour[i] & 0x00ffffffu) | (w8 << 24);
+}
+
+typedef struct { float x, y, z, w; } orc_f4;
+
+static orc_f4 soft_unpack(uint32_t t)
+{
+    orc_f4 r = {(float)(t & 255u) / 255.0f, (float)((t >> 8) & 255u) / 255.0f,
+                (float)((t >> 16) & 255u) / 255.0f, (float)(t >> 24) / 255.0f};
+    return r;
+}
+
+static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* GL_LINEAR at texture coordinate (u, v) of the 2048^2 buffer (rows from the
+ * bottom of the frame), clamped to the frame. */
+static orc_f4 soft_sample(const uint32_t* colour, const float* depth, int width, int height, float u, float v)
+{
+    float uu = u * 2048.0f - 0.5f, vv = v * 2048.0f - 0.5f;
+    float fx0 = floorf(uu), fy0 = floorf(vv);
+    float a = uu - fx0, b = vv - fy0;
+    int i0 = clampi((int)fx0, 0, width - 1), i1 = clampi((int)fx0 + 1, 0, width - 1);
+    int j0 = clampi((int)fy0, 0, height - 1), j1 = clampi((int)fy0 + 1, 0, height - 1);
+    orc_f4 t00 = soft_unpack(soft_texel(colour, depth, width, i0, height - 1 - j0));
+    orc_f4 t10 = soft_unpack(soft_texel(colour, depth, width, i1, height - 1 - j0));
+    orc_f4 t01 = soft_unpack(soft_texel(colour, depth, width, i0, height - 1 - j1));
+    orc_f4 t11 = soft_unpack(soft_texel(colour, depth, width, i1, height - 1 - j1));
+    float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    orc_f4 r;
+    r.x = w00 * t00.x + w10 * t10.x + w01 * t01.x + w11 * t11.x;
+    r.y = w00 * t00.y + w10 * t10.y + w01 * t01.y + w11 * t11.y;
+    r.z = w00 * t00.z + w10 * t10.z + w01 * t01.z + w11 * t11.z;
+    r.w = w00 * t00.w + w10 * t10.w + w01 * t01.w + w11 * t11.w;
+    return r;
+}
+
+static uint32_t soft_byte(float v)
+{
+    float f = fminf(fmaxf(v, 0.0f), 1.0f);
+    return (uint32_t)f2i(f * 255.0f + 0.5f);
+}
+
+void orc_soft_filter(const uint32_t* colour, const float* depth, int width, int height, uint32_t* out)
+{
+    /* soft.frag:12-20 and :33-34: the loops in float */
+    float circle[8][2];
+    int ncircle = 0;
+    const float step = 3.1415f * 1.9f / 6.0f;
+    for (float a = 0.0f; a < 3.1415f * 2.0f && ncircle < 8; a += step) {
+        circle[ncircle][0] = sinf(a) * 0.005f;
+        circle[ncircle][1] = cosf(a) * 0.005f;
+        ncircle++;
+    }
+    float grid[6];
+    int ngrid = 0;
+    for (float a = -1.0f; a < 1.0f && ngrid < 6; a += 2.0f / 5.0f) grid[ngrid++] = a;
+    for (int y = 0; y < height; y++)
+        for (int x = 0; x < width; x++) {
+            float u = ((float)x + 0.5f) / 2048.0f, v = ((float)y + 0.5f) / 2048.0f;
+            orc_f4 col = soft_unpack(soft_texel(colour, depth, width, x, height - 1 - y));
+            /* :11-23 largest alpha on the circle */
+            float radmax = col.w;
+            for (int i = 0; i < ncircle; i++) {
+                float w = soft_sample(colour, depth, width, height, circle[i][0] + u, circle[i][1] + v).w;
+                radmax = fmaxf(radmax, w);
+            }
+            /* :27-63 box filter of the samples near the front depth */
+            float rad = 0.0023f * radmax;
+            if (rad > 0.00008f) {
+                orc_f4 avg = col;
+                float n = 1.0f;
+                float thresh = radmax * 0.7f;
+                for (int ia = 0; ia < ngrid; ia++)
+                    for (int ib = 0; ib < ngrid; ib++) {
+                        orc_f4 c = soft_sample(colour, depth, width, height, u + grid[ia] * rad, v + grid[ib] * rad);
+                        if (c.w >= thresh) {
+                            avg.x = avg.x + c.x;
+                            avg.y = avg.y + c.y;
+                            avg.z = avg.z + c.z;
+                            avg.w = avg.w + c.w;
+                            n = n + 1.0f;
+                        }
+                    }
+                if (n > 6.0f) {
+                    float inv = 1.0f / n;
+                    col.x = avg.x * inv;
+                    col.y = avg.y * inv;
+                    col.z = avg.z * inv;
+                    col.w = avg.w * inv;
+                }
+            }
+            out[(size_t)(height - 1 - y) * width + x] =
+                soft_byte(col.x) | (soft_byte(col.y) << 8) | (soft_byte(col.z) << 16) | (soft_byte(col.w) << 24);
+        }
+}

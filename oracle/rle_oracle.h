@@ -122,6 +122,11 @@ void orc_resolve(const orc_raymap* rm, int width, int height, int rows, const ui
                  const float* raydepth, const orc_hit* rayhit, uint32_t* colour, float* depth,
                  orc_hit* hit, int64_t* sample_index);
 
+/* bin/shader/soft.frag over the colorize pass's frame buffer, one resolved
+ * frame (RGBA8 colour + float depth as orc_resolve writes them) in, RGBA8
+ * out; bilinear taps in single precision, clamped to the frame. */
+void orc_soft_filter(const uint32_t* colour, const float* depth, int width, int height, uint32_t* out);
+
 /* Rows the reference's ray buffer has (RAYS_CASTED = 4*maxres, src/main.cpp:459)
  * and the rays a frame renders into it: min(sum res, rows). */
 int orc_raybuf_rows(const orc_raymap* rm);

@@ -155,6 +155,7 @@ def _load() -> C.CDLL:
         "rle_scenegen_dense": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, vp, vp]),
         "rle_host_free": (None, [vp]),
         "rle_scenegen_device": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, C.POINTER(vp)]),
+        "rle_soft_filter": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp]),
         "rle_encode_device": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
         "rle_raymap_build": (C.c_int, [C.POINTER(Camera), C.POINTER(ViewParams), C.POINTER(RayMap)]),
         "rle_raybuf_words": (C.c_size_t, [C.POINTER(RayMap)]),
@@ -545,6 +546,12 @@ def render_frame_noalloc(scene: Scene, cam: Camera, view: ViewParams, colour, de
     bytes per device).  Calls share that array, so keep them on one stream."""
     _check(_lib.rle_render_frame_noalloc(scene.handle, C.byref(cam), C.byref(view), ptr(colour), ptr(depth),
                                          stream or None), "rle_render_frame_noalloc")
+
+
+def soft_filter(colour, depth, width: int, height: int, out, stream: int = 0) -> None:
+    """rle_soft_filter: the reference's soft post-filter (bin/shader/soft.frag)
+    over one resolved frame; RGBA8 out (must not alias colour)."""
+    _check(_lib.rle_soft_filter(ptr(colour), ptr(depth), width, height, ptr(out), stream or None), "rle_soft_filter")
 
 
 def render_frame_noalloc_limit() -> int:

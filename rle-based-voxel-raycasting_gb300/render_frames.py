@@ -1,0 +1,105 @@
+"""Render frames of a seeded scene from the command line.
+
+    python rle-based-voxel-raycasting_gb300/render_frames.py [--size 2048] [--height 256] [--seed 2]
+        [--width 1920] [--screen-height 1080] [--frames 6] [--fov 90] [--png-dir DIR]
+
+Builds the scene on the GPU (rle_scenegen_device), walks a seeded camera
+path (poses 10-80 voxels above the ground, yaw uniform, pitch up to 30
+degrees) and renders each frame with rle_render_frame, printing the time per
+frame; with --png-dir it also writes every frame as a PNG.  This is the
+headless counterpart of the reference's interactive viewer
+(src/main.cpp:446-669): the frame ends in device buffers, not in a window.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import struct
+import sys
+import time
+import zlib
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+
+
+def _package():
+    if "rle_gb300" in sys.modules:
+        return sys.modules["rle_gb300"]
+    spec = importlib.util.spec_from_file_location("rle_gb300", PKG / "__init__.py",
+                                                  submodule_search_locations=[str(PKG)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["rle_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def write_png(path: Path, rgb: np.ndarray) -> None:
+    """8-bit RGB image (h x w x 3) as a PNG (zlib-compressed scanlines)."""
+    h, w, _ = rgb.shape
+    raw = b"".join(b"\x00" + rgb[y].tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    path.write_bytes(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)) +
+                     chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--size", type=int, default=2048, help="scene columns along x and z (power of two)")
+    ap.add_argument("--height", type=int, default=256, help="scene height in voxels (multiple of 64)")
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--no-caves", action="store_true")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--screen-height", type=int, default=1080)
+    ap.add_argument("--fov", type=float, default=90.0)
+    ap.add_argument("--frames", type=int, default=6)
+    ap.add_argument("--path-seed", type=int, default=20261203)
+    ap.add_argument("--png-dir", type=str, default=None)
+    args = ap.parse_args(argv)
+
+    import torch
+
+    rle = _package()
+    if not torch.cuda.is_available():
+        print("render_frames: no CUDA device", file=sys.stderr)
+        return 2
+    p = rle.scenegen_default(args.size, args.height, args.size, args.seed, caves=not args.no_caves)
+    scene = rle.Scene.generate_on_device(p)
+    info = scene.info()
+    table, words = scene.copy_level(0)
+    rng = np.random.default_rng(args.path_seed)
+    W, H = args.width, args.screen_height
+    view = rle.view_params(W, H)
+    ws_bytes = rle.frame_workspace_bytes(view)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    colour = torch.empty(W * H, dtype=torch.int32, device="cuda")
+    depth = torch.empty(W * H, dtype=torch.float32, device="cuda")
+    out_dir = Path(args.png_dir) if args.png_dir else None
+    if out_dir:
+        out_dir.mkdir(parents=True, exist_ok=True)
+    for i in range(args.frames):
+        x, z = rng.uniform(0, info.sx[0]), rng.uniform(0, info.sz[0])
+        g = rle.ground_height(table, words, info.sx[0], info.sy[0], int(x), int(z))
+        pitch = float(rng.uniform(1.0, 30.0) * rng.choice([-1.0, 1.0]))
+        cam = rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)), pitch,
+                         args.fov, scene_height=info.sy[0])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rle.render_frame(scene, cam, view, ws, ws_bytes, colour, depth)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"frame {i}: {e0.elapsed_time(e1):.3f} ms", flush=True)
+        if out_dir:
+            rgba = colour.cpu().numpy().view(np.uint8).reshape(H, W, 4)
+            write_png(out_dir / f"frame_{i:04d}.png", np.ascontiguousarray(rgba[:, :, :3]))
+    scene.free()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
