@@ -306,7 +306,8 @@ typedef struct rle_frame_request {
 } rle_frame_request;
 
 typedef struct rle_batch_tuning {
-    int tile_rays;          /* rays per work tile: 1..256 (autotuned over 8, 16, 32, 64) */
+    int tile_rays;          /* most rays a lane group claims at once: 1..256 (default 1;
+                               claims shrink further as the queue drains) */
     int lanes_per_ray;      /* lanes cooperating on one column ray: 8, 16, 32 */
     int staging;            /* staging depth: tiles a lane group claims per grab, 1..8 */
     int threads_per_block;  /* 32, 64, 96 or 128 */
@@ -328,7 +329,7 @@ size_t rle_batch_words_needed(const rle_frame_request* frames, int n);
 rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                             void* stream);
 /* Times every tile_rays x lanes_per_ray x staging combination
- * ({8,16,32,64} x {8,16,32} x {1,2,3}) on these frames (median of `repeats`
+ * ({1,2,4,8,16,32,64} x {8,16,32} x {1,2,3}) on these frames (median of `repeats`
  * runs each), keeps the fastest as the batch's tuning and returns it. */
 rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                               int repeats, rle_batch_tuning* best, float* best_ms);

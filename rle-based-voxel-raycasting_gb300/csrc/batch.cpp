@@ -63,7 +63,7 @@ struct rle_batch {
     int parity = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    rle_batch_tuning tuning{16, 32, 1, 128, 1};
+    rle_batch_tuning tuning{1, 32, 1, 128, 1};
     int raycast_blocks = 0;
     int resolve_blocks = 0;
     std::mutex mu;
@@ -400,7 +400,7 @@ extern "C" rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, c
     rle_batch_tuning win = start;
     float win_ms = 1e30f;
     rle_status st = RLE_OK;
-    const int tiles[] = {8, 16, 32, 64}, lanes[] = {8, 16, 32}, stagings[] = {1, 2, 3};
+    const int tiles[] = {1, 2, 4, 8, 16, 32, 64}, lanes[] = {8, 16, 32}, stagings[] = {1, 2, 3};
     for (int lv : lanes) {
         for (int tv : tiles) {
             for (int sv : stagings) {
