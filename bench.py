@@ -51,6 +51,20 @@ def load_rle():
     return mod
 
 
+def pow2_ceil(v: int) -> int:
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
+
+
+def frame_view(rle, w: int, h: int, **kw):
+    """A frame of w x h pixels mapped onto the reference's geometry as the
+    configs define it: maxres = w (RAYS_CASTED_RES = 4w), samples per column
+    ray = the smallest power of two >= w (RENDER_SIZE), border (w-h)/(2w)."""
+    return rle.view_params(w, h, samples=pow2_ceil(w), **kw)
+
+
 def scene_bytes(rle):
     p = rle.scenegen_default(SCENE["n"], SCENE["sy"], SCENE["n"], SCENE["seed"], caves=SCENE["caves"])
     return rle.scenegen_rle4(p)
@@ -156,7 +170,7 @@ def run_ours(args):
     table, words = scene.copy_level(0)
     lv0 = (info.sx[0], info.sy[0], info.sz[0], table, words)
     cams = poses(rle, lv0, args.warmup + args.steps, seed=20261203 + rank)
-    view = rle.view_params(W, H)
+    view = frame_view(rle, W, H)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     ws_bytes = rle.frame_workspace_bytes(view)
@@ -316,7 +330,7 @@ def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
     with CUDA events on one stream; primary rays = pixels of all 64 frames."""
     rng = np.random.default_rng(seed)
     cams = poses(rle, lv0, n_cams, seed=seed)
-    views = [rle.view_params(*BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]) for _ in range(n_cams)]
+    views = [frame_view(rle, *BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]) for _ in range(n_cams)]
     pixels = sum(v.width * v.height for v in views)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
@@ -334,7 +348,8 @@ def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
         for c, v, (col, dep) in zip(cams, views, outs):
             rle.render_frame(scene, c, v, ws, ws_bytes, col, dep, None, stream=sp)
 
-    batch = rle.Batch(max_frames=n_cams, raybuf_words=rle.batch_words_needed(reqs), max_samples=1920)
+    batch = rle.Batch(max_frames=n_cams, raybuf_words=rle.batch_words_needed(reqs),
+                      max_samples=max(v.samples for v in views))
     t_tune = time.perf_counter()
     best, best_ms = batch.autotune(scene, reqs, repeats=2)
     t_tune = time.perf_counter() - t_tune
@@ -399,7 +414,7 @@ def run_config5(rle, torch, frames=120, views_per_batch=8, seed=7, repeats=3):
         cams.append(rle.camera(float(x), float(z), g + float(rng.uniform(20, 200)), float(rng.uniform(0, 360)),
                                float(rng.uniform(1, 30) * rng.choice([-1, 1])), 75.0, scene_height=512))
     W4, H4 = 3840, 2160
-    view = rle.view_params(W4, H4, mip_distance=256)
+    view = frame_view(rle, W4, H4, mip_distance=256)
     stream = torch.cuda.Stream()
     sp = stream.cuda_stream
     outs = [(torch.empty(W4 * H4, dtype=torch.int32, device="cuda"),
@@ -484,7 +499,7 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
         sid = int(rng.integers(0, len(scenes)))
         (w, h) = SERVE_RES[int(rng.choice(len(SERVE_RES), p=probs))][0]
         cam = poses(rle, levels[sid], 1, seed=seed + 7 * i + 1)[0]
-        reqs.append((sid, cam, rle.view_params(w, h)))
+        reqs.append((sid, cam, frame_view(rle, w, h)))
     ring = 64  # output buffers reused round-robin
     outs = [(torch.empty(1920 * 1080, dtype=torch.int32, device="cuda"),
              torch.empty(1920 * 1080, dtype=torch.float32, device="cuda")) for _ in range(ring)]
@@ -494,7 +509,7 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
                           f"resolution mix 256^2:.4 640x480:.3 1280x720:.2 1920x1080:.1, HBM budget 120 GB"}
     for mode in ("batched", "plain"):
         srv = rle.Server(hbm_budget_bytes=120 << 30, raybuf_words=32 << 20, max_frames_per_batch=64,
-                         max_inflight=3, max_samples=1920, plain=(mode == "plain"))
+                         max_inflight=3, max_samples=2048, plain=(mode == "plain"))
         for sc in scenes:
             srv.add_scene(sc)
         # warm-up: one of each resolution
@@ -535,7 +550,7 @@ def cpu_baseline(rle, data, cams):
     from oracle import pyoracle as po
     po.build_oracle()
     oscene = po.OracleScene.from_rle4(data)
-    view = rle.view_params(W, H)
+    view = frame_view(rle, W, H)
     threads = os.cpu_count() or 1
     t = 0.0
     for c in cams:
@@ -563,7 +578,7 @@ def run_reference(args):
     oscene = po.OracleScene.from_rle4(data)
     sx, sy, sz, table, words = oscene.levels[0]
     cams = poses(rle, (sx, sy, sz, table, words), args.warmup + args.steps)
-    view = rle.view_params(W, H)
+    view = frame_view(rle, W, H)
     threads = os.cpu_count() or 1
 
     def frame(c):

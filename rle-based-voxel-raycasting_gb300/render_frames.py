@@ -57,6 +57,8 @@ def main(argv=None) -> int:
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--screen-height", type=int, default=1080)
     ap.add_argument("--fov", type=float, default=90.0)
+    ap.add_argument("--samples", type=int, default=0,
+                    help="samples per column ray (default: the smallest power of two >= width)")
     ap.add_argument("--frames", type=int, default=6)
     ap.add_argument("--path-seed", type=int, default=20261203)
     ap.add_argument("--png-dir", type=str, default=None)
@@ -74,7 +76,12 @@ def main(argv=None) -> int:
     table, words = scene.copy_level(0)
     rng = np.random.default_rng(args.path_seed)
     W, H = args.width, args.screen_height
-    view = rle.view_params(W, H)
+    samples = args.samples
+    if samples <= 0:
+        samples = 1
+        while samples < W:
+            samples <<= 1
+    view = rle.view_params(W, H, samples=samples)
     ws_bytes = rle.frame_workspace_bytes(view)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
     colour = torch.empty(W * H, dtype=torch.int32, device="cuda")
