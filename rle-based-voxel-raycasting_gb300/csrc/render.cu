@@ -575,13 +575,101 @@ __device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int 
     return n != 0;
 }
 
+// Short spans are not filled when the merge reaches them: the merge claims
+// their samples in the occupancy mask (the samples still free at that
+// moment, exactly those the fill would colour) and queues the span; a
+// flush then colours the queued samples of up to G spans G at a time, one
+// sample per lane.  A span of at most kShortSpan samples lies in two mask
+// words, and a sample m places into its span needs m accumulation steps,
+// which the lane replays from the span's start.  Longer spans are filled at
+// once by draw_span.  Queue entry: 4 x float4 in shared memory.
+constexpr int kShortSpan = 32;
+
+struct SpanQueue {
+    float4* e;  // G entries of this ray
+    int n;
+};
+
+template <int G>
+__device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, unsigned gmask, int k, uint32_t* row,
+                                            float* drow, rle_hit* hrow, Pending& pend) {
+    if (q.n == 0) return;
+    const int lb = lane_base(gmask);
+    // samples per queued span, inclusive prefix over the group's lanes
+    int cnt = 0;
+    if (k < q.n) {
+        const float4 e0 = q.e[4 * k];
+        cnt = __popc(__float_as_uint(e0.z)) + __popc(__float_as_uint(e0.w));
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) {
+        const int v = __shfl_up_sync(gmask, incl, o);
+        if (k >= o) incl += v;
+    }
+    const int total = __shfl_sync(gmask, incl, lb + q.n - 1);
+    for (int b = 0; b < total; b += G) {
+        const int t = b + k;
+        // span of sample t: the first entry whose inclusive count exceeds t
+        int lo = 0, hi = q.n - 1;
+#pragma unroll
+        for (int it = 0; (1 << it) < G; it++) {
+            const int mid = (lo + hi) >> 1;
+            const int v = __shfl_sync(gmask, incl, lb + mid);
+            if (lo < hi) {
+                if (v > t) hi = mid;
+                else lo = mid + 1;
+            }
+        }
+        const int before = __shfl_sync(gmask, incl - cnt, lb + lo);
+        if (t < total) {
+            const float4 e0 = q.e[4 * lo], e1 = q.e[4 * lo + 1], e2 = q.e[4 * lo + 2], e3 = q.e[4 * lo + 3];
+            const uint32_t own0 = __float_as_uint(e0.z), own1 = __float_as_uint(e0.w);
+            const int r = t - before, c0 = __popc(own0);
+            const int bit = r < c0 ? static_cast<int>(__fns(own0, 0, r + 1)) : 32 + static_cast<int>(__fns(own1, 0, r - c0 + 1));
+            const int y = __float_as_int(e0.x);
+            const int p = __float_as_int(e0.y) + bit;  // base + bit
+            const float u2dz = e1.z, onedz2 = e2.x;
+            const float mult = static_cast<float>(y + 1) - e1.x;
+            float uz = e1.y + u2dz * mult;
+            float onez = e1.w + onedz2 * mult;
+            for (int j = y; j < p; j++) {
+                uz += u2dz;
+                onez += onedz2;
+            }
+            const int texture = __float_as_int(e2.z);
+            const int mip = __float_as_int(e3.y);
+            const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(uz / onez, static_cast<float>(texture)), e2.y));
+            const float depth = 1 / onez;
+            const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
+            pend.flush();
+            pend.at = &row[p];
+            pend.colour = __ldg(&P.slabs[mip][__float_as_uint(e3.x) + u]);
+            pend.z = real_z << 16;
+            drow[p] = depth;
+            if (hrow) {
+                const uint32_t vxz = __float_as_uint(e3.z);
+                rle_hit h;
+                h.x = static_cast<uint16_t>(vxz & 0xffffu);
+                h.z = static_cast<uint16_t>(vxz >> 16);
+                h.y = static_cast<uint16_t>((__float_as_int(e2.w) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
+                h.mip = static_cast<uint8_t>(mip);
+                h.flags = 1;
+                hrow[p] = h;
+            }
+        }
+    }
+    __syncwarp(gmask);  // the entries are rewritten by the next spans
+    q.n = 0;
+}
+
 // The exact walk over the runs prepare_cell recorded for one cell (same
 // tests, same order, same horizon updates as merge_cell).
 template <int G>
 __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& mask, unsigned gmask, int k,
                                                uint32_t* row, float* drow, rle_hit* hrow, const float4* rec, int nrec,
                                                float pz, float py, int mip, int vx, int vz, int& ymin, int& ymax,
-                                               Pending& pend, Counts& cnt) {
+                                               Pending& pend, SpanQueue& q, Counts& cnt) {
     const float res_y2 = static_cast<float>(P.S / 2);
     // clip top (:467)
     if (pz * res_y2 + py <= pz * static_cast<float>(ymin)) return;
@@ -612,6 +700,30 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
         sp.umax = d.y;
         sp.texture = __float_as_int(d.z);
         sp.sg0 = __float_as_int(d.w);
+        if (scr_y2 - y <= kShortSpan) {
+            // claim the free samples of [y, scr_y2) now, colour them later
+            if (q.n == G) flush_spans<G>(P, q, gmask, k, row, drow, hrow, pend);
+            const int base = y & ~31, wi = base >> 5;
+            const int hi_bits = scr_y2 - base - 32;  // samples in the second word (<= 31)
+            const uint32_t r0 = (hi_bits >= 0 ? 0xffffffffu : ((1u << (scr_y2 - base)) - 1u)) & (0xffffffffu << (y - base));
+            const uint32_t r1 = hi_bits > 0 ? ((1u << hi_bits) - 1u) : 0u;
+            const uint32_t m0 = mask.w[wi], m1 = r1 ? mask.w[wi + 1] : 0u;
+            const uint32_t own0 = r0 & ~m0, own1 = r1 & ~m1;
+            __syncwarp(gmask);
+            if (k == 0) {
+                mask.w[wi] = m0 | r0;
+                if (r1) mask.w[wi + 1] = m1 | r1;
+                float4* e = q.e + 4 * q.n;
+                e[0] = make_float4(__int_as_float(y), __int_as_float(base), __uint_as_float(own0), __uint_as_float(own1));
+                e[1] = b;
+                e[2] = d;
+                e[3] = make_float4(__uint_as_float(__float_as_uint(a.w)), __int_as_float(mip),
+                                   __uint_as_float(static_cast<uint32_t>(vx) | (static_cast<uint32_t>(vz) << 16)), 0.0f);
+            }
+            __syncwarp(gmask);
+            q.n++;
+            continue;
+        }
         const uint16_t* colours = P.slabs[mip] + __float_as_uint(a.w);
         draw_span<G, false>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, mip, vx, vz, pend, cnt);
     }
@@ -733,13 +845,14 @@ __device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, fl
 // chunks of G DDA steps, lane k taking step k of each.
 template <int G, bool kCount, bool kHits>
 __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, float4* recs,
-                                         int k, unsigned gmask, Counts& cnt) {
+                                         float4* spans, int k, unsigned gmask, Counts& cnt) {
     const int S = P.S;
     const int words = (S + 31) >> 5;
     Mask mask{mask_words};
 
     float4* my_recs = recs + static_cast<size_t>(threadIdx.x) * (3 * kRecs);
     Pending pend;
+    SpanQueue q{spans, 0};
     Ray R;
     Walk W;
     bool live = false;
@@ -844,7 +957,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                     const float4* rec = recs + static_cast<size_t>((threadIdx.x & ~31u) + src) * (3 * kRecs);
                     const int ymin_before = ymin;
                     merge_recorded<G>(P, mask, gmask, k, row, drow, hrow, rec, nrec, pz, py, mip, vx, vz, ymin, ymax,
-                                      pend, cnt);
+                                      pend, q, cnt);
                     if (ymin != ymin_before) {
                         // cells whose first recorded run now breaks the walk
                         // at once are no-ops: drop them all in one vote
@@ -865,6 +978,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             nvalid = nvalid_next;
         }
     }
+    flush_spans<G>(P, q, gmask, k, row, drow, hrow, pend);
     pend.flush();
     __syncwarp();
 
@@ -897,8 +1011,10 @@ __host__ __device__ __forceinline__ int mask_region_words(int slots, int words) 
     return (slots * words + 3) & ~3;
 }
 __host__ __device__ __forceinline__ size_t raycast_smem_bytes(int threads, int slots, int words) {
+    // masks | run records (kRecs per thread) | span queues (32 / slots-per-warp entries per ray,
+    // i.e. one per lane of the group: as many entries per block as threads)
     return static_cast<size_t>(mask_region_words(slots, words)) * 4 +
-           static_cast<size_t>(threads) * kRecs * 3 * sizeof(float4);
+           static_cast<size_t>(threads) * kRecs * 3 * sizeof(float4) + static_cast<size_t>(threads) * 4 * sizeof(float4);
 }
 
 // Lane layout of a group of G lanes within a block.
@@ -926,8 +1042,9 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
     const int x = blockIdx.x * rays_per_block + L.slot;
     const int words = (P.S + 31) >> 5;
     float4* recs = reinterpret_cast<float4*>(smem + mask_region_words(rays_per_block, words));
+    float4* spans = recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (4 * G);
     Counts cnt;
-    cast_ray<G, kCount, kHits>(P, x, x < P.rays, smem + L.slot * words, recs, L.k, L.gmask, cnt);
+    cast_ray<G, kCount, kHits>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, cnt);
 }
 
 // Many frames in one persistent launch.  The rays of all frames form one
@@ -945,6 +1062,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
     uint32_t* mask_words = smem + L.slot * max_words;
     float4* recs = reinterpret_cast<float4*>(
         smem + mask_region_words((static_cast<int>(blockDim.x) >> 5) * (32 / G), max_words));
+    float4* spans = recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (4 * G);
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
     // Guided self-scheduling: a group claims up to tile * staging rays, but
@@ -973,7 +1091,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 }
                 f = lo;
             }
-            cast_ray<G, false, kHits>(frames[f], r - ray_start[f], true, mask_words, recs, L.k, L.gmask, cnt);
+            cast_ray<G, false, kHits>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k, L.gmask, cnt);
         }
     }
 }
