@@ -154,6 +154,21 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
+def replica_throughput(local_ms: float, local_units: float, dist=None, device: str = "cuda"):
+    """Replicas (no exchange step): every rank renders its own frames.  The
+    job's time is the slowest rank's, its work the sum over ranks; returns
+    (mega-units per second, job milliseconds)."""
+    ms, units = float(local_ms), float(local_units)
+    if dist is not None and dist.is_initialized() and dist.get_world_size() > 1:
+        import torch
+        t_max = torch.tensor([ms], dtype=torch.float64, device=device)
+        t_sum = torch.tensor([units], dtype=torch.float64, device=device)
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t_sum, op=dist.ReduceOp.SUM)
+        ms, units = float(t_max.item()), float(t_sum.item())
+    return units / (ms / 1e3) / 1e6, ms
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -210,13 +225,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
     frame_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(frame_ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    pixels = W * H * args.steps * world
-    value = pixels / (total_ms / 1e3) / 1e6
+    value, total_ms = replica_throughput(sum(frame_ms), W * H * args.steps, dist, device="cuda")
 
     # ---- raycast kernel alone, same frames, with work counters (roofline) ----
     words = rle.raybuf_words(rms[0])
