@@ -165,3 +165,48 @@ def test_cancel_timeout_and_injected_failures(rle, scenes, torch_cuda):
     t = srv.submit(0, reqs[0][1], reqs[0][2], bufs[0][0], bufs[0][1])
     assert srv.wait(t, 20000).status == 0
     srv.destroy()
+
+
+def test_concurrent_submitters(rle, scenes, torch_cuda):
+    """Four host threads submit and wait at once; every result equals the
+    request rendered alone and every ticket completes exactly once."""
+    import threading
+    torch = torch_cuda
+    srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
+                     max_samples=640)
+    for s in scenes:
+        srv.add_scene(s)
+    reqs = _requests(rle, scenes, 32, 21)
+    bufs = _buffers(torch, reqs)
+    torch.cuda.synchronize()
+    statuses = {}
+    errors = []
+
+    def worker(t):
+        try:
+            mine = list(range(t, len(reqs), 4))
+            tickets = []
+            for i in mine:
+                sid, cam, view = reqs[i]
+                tickets.append((i, srv.submit(sid, cam, view, bufs[i][0], bufs[i][1])))
+            for i, tk in tickets:
+                statuses[i] = srv.wait(tk, 20000).status
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join(60)
+    assert not errors, errors
+    assert sorted(statuses) == list(range(len(reqs))) and set(statuses.values()) == {0}
+    srv.drain(20000)
+    torch.cuda.synchronize()
+    for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
+        wc, wd = _alone(rle, torch, scenes[sid], cam, view)
+        assert np.array_equal(c.cpu().numpy().view(np.uint32), wc), f"request {i} colour"
+        assert np.array_equal(d.cpu().numpy().view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+    st = srv.stats()
+    assert st.submitted == 32 and st.completed == 32 and st.failed == 0
+    srv.destroy()
