@@ -114,6 +114,23 @@ rle_status rle_scenegen_dense(const rle_scenegen_params* p, int mip, uint8_t* bi
                               uint16_t* colours);
 void rle_host_free(void* p);
 
+/* Range-checked debug build (build.py --bounds-check ->
+ * librle_gb300_checked.so): every column-table, slab and ray-buffer index
+ * the kernels use is checked; a failed check is recorded and the access
+ * skipped.  Reads (and with clear != 0 resets) the record of `device`:
+ * out4[0] = OR of the failed checks (1 column table, 2 run header, 4 colour
+ * word, 8 ray-buffer sample, 16 resolve fetch), out4[1..2] = low and high
+ * words of the first failing index.  RLE_ERR_UNSUPPORTED in the regular
+ * build.  No reference counterpart (the reference has no such mode). */
+rle_status rle_bounds_check_read(int device, uint32_t* out4, int clear);
+/* Debug build only: device pointers of one level's column table and slab
+ * words and the level's word count, for tests that corrupt a resident scene
+ * on purpose (the checked build then has to refuse the bad indices).  The
+ * checked build pads every level's words with 64 KB of zeros.
+ * RLE_ERR_UNSUPPORTED in the regular build. */
+rle_status rle_debug_level_pointers(const rle_scene* scene, int mip, void** table, void** slabs,
+                                    uint64_t* words);
+
 /* ---------------------------------------------------------------------- */
 /* Soft post-filter                                                       */
 /* ---------------------------------------------------------------------- */

@@ -17,13 +17,16 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from pathlib import Path
 from typing import Optional
 
 import numpy as np
 
 _HERE = Path(__file__).resolve().parent
-LIB_PATH = _HERE / "librle_gb300.so"
+# RLE_GB300_LIB selects another build of the library (the range-checked
+# debug build, librle_gb300_checked.so); the default is the regular one.
+LIB_PATH = Path(os.environ["RLE_GB300_LIB"]) if os.environ.get("RLE_GB300_LIB") else _HERE / "librle_gb300.so"
 RLE_MAX_MIPS = 8
 # rotation.x of the reference grows as the view turns down (src/RayMap.h:121);
 # camera() takes pitch with negative = down.
@@ -156,6 +159,8 @@ def _load() -> C.CDLL:
         "rle_host_free": (None, [vp]),
         "rle_scenegen_device": (C.c_int, [C.POINTER(ScenegenParams), C.c_int, C.POINTER(vp)]),
         "rle_soft_filter": (C.c_int, [vp, vp, C.c_int, C.c_int, vp, vp]),
+        "rle_bounds_check_read": (C.c_int, [C.c_int, C.POINTER(C.c_uint32), C.c_int]),
+        "rle_debug_level_pointers": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_uint64)]),
         "rle_encode_device": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]),
         "rle_raymap_build": (C.c_int, [C.POINTER(Camera), C.POINTER(ViewParams), C.POINTER(RayMap)]),
         "rle_raybuf_words": (C.c_size_t, [C.POINTER(RayMap)]),
@@ -552,6 +557,23 @@ def soft_filter(colour, depth, width: int, height: int, out, stream: int = 0) ->
     """rle_soft_filter: the reference's soft post-filter (bin/shader/soft.frag)
     over one resolved frame; RGBA8 out (must not alias colour)."""
     _check(_lib.rle_soft_filter(ptr(colour), ptr(depth), width, height, ptr(out), stream or None), "rle_soft_filter")
+
+
+def bounds_check_read(device: int = 0, clear: bool = True) -> tuple[int, int]:
+    """(failed-check flags, first failing index) of the range-checked debug
+    library; raises RLEError(UNSUPPORTED) with the regular library."""
+    out = (C.c_uint32 * 4)()
+    _check(_lib.rle_bounds_check_read(device, out, int(clear)), "rle_bounds_check_read")
+    return int(out[0]), int(out[1]) | (int(out[2]) << 32)
+
+
+def debug_level_pointers(scene: "Scene", mip: int) -> tuple[int, int, int]:
+    """(table, slabs, words) device pointers of a level (range-checked debug
+    library only)."""
+    t, sl, w = C.c_void_p(), C.c_void_p(), C.c_uint64()
+    _check(_lib.rle_debug_level_pointers(scene.handle, mip, C.byref(t), C.byref(sl), C.byref(w)),
+           "rle_debug_level_pointers")
+    return int(t.value), int(sl.value), int(w.value)
 
 
 def render_frame_noalloc_limit() -> int:

@@ -1,7 +1,7 @@
 """Builds librle_gb300.so in place: CUDA sources for sm_103a with nvcc,
 host C++ with g++, linked against the static CUDA runtime.
 
-    python rle-based-voxel-raycasting_gb300/build.py [--jobs N] [--force]
+    python rle-based-voxel-raycasting_gb300/build.py [--jobs N] [--force] [--bounds-check]
 
 Floating point: the traversal and resolve kernels are compiled with
 -fmad=false, IEEE division and square root and no flush-to-zero; host code
@@ -25,6 +25,10 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "librle_gb300.so"
+# Debug variant: every device table, slab and ray-buffer index range-checked
+# (-DRLE_BOUNDS_CHECK); a failed check is recorded, not executed.
+BUILD_CHECKED = PKG / "_build_checked"
+LIB_CHECKED = PKG / "librle_gb300_checked.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -77,16 +81,17 @@ def _stale(obj: Path, src: Path) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -> Path:
+def build(jobs: int | None = None, force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
     home = cuda_home()
     nvcc = str(home / "bin" / "nvcc")
-    BUILD.mkdir(exist_ok=True)
+    bdir, lib = (BUILD_CHECKED, LIB_CHECKED) if checked else (BUILD, LIB)
+    bdir.mkdir(exist_ok=True)
     cu, cpp = sources()
-    common_inc = [f"-I{INCLUDE}", f"-I{CSRC}"]
+    common_inc = [f"-I{INCLUDE}", f"-I{CSRC}"] + (["-DRLE_BOUNDS_CHECK"] if checked else [])
     steps = []
     objs = []
     for src in cu:
-        obj = BUILD / (src.stem + ".cu.o")
+        obj = bdir / (src.stem + ".cu.o")
         objs.append(obj)
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
                "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -94,7 +99,7 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
         if force or _stale(obj, src):
             steps.append(cmd)
     for src in cpp:
-        obj = BUILD / (src.stem + ".cpp.o")
+        obj = bdir / (src.stem + ".cpp.o")
         objs.append(obj)
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
                "-Wall", *common_inc, f"-I{home / 'include'}", "-c", str(src), "-o", str(obj)]
@@ -102,15 +107,15 @@ def build(jobs: int | None = None, force: bool = False, verbose: bool = False) -
             steps.append(cmd)
     with cf.ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
         list(ex.map(_run, steps))
-    if steps or not LIB.exists() or foreign_binary(LIB):
+    if steps or not lib.exists() or foreign_binary(lib):
         lib_dirs = [home / "lib64", home / "lib", home / "targets" / "sbsa-linux" / "lib",
                     home / "targets" / "x86_64-linux" / "lib"]
         ldirs = [f"-L{d}" for d in lib_dirs if d.exists()]
-        tmp = LIB.with_suffix(".so.tmp")
+        tmp = lib.with_suffix(".so.tmp")
         _run(["g++", "-shared", "-fopenmp", "-o", str(tmp), *map(str, objs), *ldirs,
               "-lcudart_static", "-lrt", "-ldl", "-lpthread"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 def main(argv: list[str] | None = None) -> int:
@@ -118,9 +123,11 @@ def main(argv: list[str] | None = None) -> int:
     ap.add_argument("--jobs", type=int, default=None)
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--verbose", action="store_true", help="pass -Xptxas -v (registers, spills)")
+    ap.add_argument("--bounds-check", action="store_true",
+                    help="build the range-checked debug library librle_gb300_checked.so")
     a = ap.parse_args(argv)
     try:
-        lib = build(a.jobs, a.force, a.verbose)
+        lib = build(a.jobs, a.force, a.verbose, a.bounds_check)
     except RuntimeError as e:
         print(e, file=sys.stderr)
         return 1

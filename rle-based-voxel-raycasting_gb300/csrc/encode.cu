@@ -589,11 +589,12 @@ rle_status encode_levels(Build& B, WriteArgs base, rle_scene** out) {
         D.sz = L.sz;
         D.words = words;
         const size_t tbytes = static_cast<size_t>(n) * 8;
-        const size_t sbytes = static_cast<size_t>(words) * 2 + 16;
+        const size_t sbytes = static_cast<size_t>(words) * 2 + rle::kSlabPadBytes;
         if ((e = cudaMalloc(&D.d_table, tbytes)) != cudaSuccess) { st = cuda_fail(e, "scene build: cudaMalloc(table)"); break; }
         if ((e = cudaMalloc(&D.d_slabs, sbytes)) != cudaSuccess) { st = cuda_fail(e, "scene build: cudaMalloc(slabs)"); break; }
         // zero padding after the words (the writer covers every word)
-        if ((e = cudaMemsetAsync(reinterpret_cast<char*>(D.d_slabs) + words * 2, 0, 16, B.stream)) != cudaSuccess) {
+        if ((e = cudaMemsetAsync(reinterpret_cast<char*>(D.d_slabs) + words * 2, 0, rle::kSlabPadBytes, B.stream)) !=
+            cudaSuccess) {
             st = cuda_fail(e, "scene build: cudaMemsetAsync(padding)");
             break;
         }

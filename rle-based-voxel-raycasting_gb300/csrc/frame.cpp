@@ -70,6 +70,8 @@ rle_status fill_ray_params(const rle_scene* scene, const rle_raymap* rm, RayPara
     for (int m = 0; m < scene->nummaps; m++) {
         p->table[m] = reinterpret_cast<const uint2*>(scene->lv[m].d_table);
         p->slabs[m] = scene->lv[m].d_slabs;
+        p->slab_words[m] = scene->lv[m].words;
+        p->table_cols[m] = static_cast<uint32_t>(static_cast<uint64_t>(scene->lv[m].sx) * scene->lv[m].sz);
     }
     return RLE_OK;
 }
@@ -261,4 +263,45 @@ extern "C" rle_status rle_render_frame(const rle_scene* scene, const rle_camera*
     if (st != RLE_OK) return st;
     rle::DeviceGuard g(scene->device);
     return rle_resolve(&rm, raybuf, raydepth, rayhit, d_colour, d_depth, d_hit, stream);
+}
+
+extern "C" rle_status rle_bounds_check_read(int device, uint32_t* out4, int clear) {
+    if (!out4) return RLE_ERR_INVALID_ARG;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) {
+        rle::set_error("rle_bounds_check_read: device %d", device);
+        return RLE_ERR_INVALID_ARG;
+    }
+    unsigned a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
+    const bool ok = rle::bounds_render(a, clear != 0) && rle::bounds_resolve(b, clear != 0);
+    if (prev >= 0) cudaSetDevice(prev);
+    if (!ok) {
+        rle::set_error("rle_bounds_check_read: this library was built without RLE_BOUNDS_CHECK");
+        return RLE_ERR_UNSUPPORTED;
+    }
+    out4[0] = a[0] | b[0];
+    out4[1] = a[0] ? a[1] : b[1];
+    out4[2] = a[0] ? a[2] : b[2];
+    out4[3] = 0;
+    return RLE_OK;
+}
+
+extern "C" rle_status rle_debug_level_pointers(const rle_scene* scene, int mip, void** table, void** slabs,
+                                               uint64_t* words) {
+#ifdef RLE_BOUNDS_CHECK
+    if (!scene || mip < 0 || mip >= scene->nummaps || !table || !slabs || !words) return RLE_ERR_INVALID_ARG;
+    *table = scene->lv[mip].d_table;
+    *slabs = scene->lv[mip].d_slabs;
+    *words = scene->lv[mip].words;
+    return RLE_OK;
+#else
+    (void)scene;
+    (void)mip;
+    (void)table;
+    (void)slabs;
+    (void)words;
+    rle::set_error("rle_debug_level_pointers: this library was built without RLE_BOUNDS_CHECK");
+    return RLE_ERR_UNSUPPORTED;
+#endif
 }

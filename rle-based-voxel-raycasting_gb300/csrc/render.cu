@@ -42,6 +42,26 @@ namespace {
 
 constexpr uint32_t kSky = 0x00ff8844u;
 
+// Debug builds with RLE_BOUNDS_CHECK range-check every column-table, slab
+// and ray-buffer index: a failed check records its code (and the first
+// index) in g_bounds and skips the access (reads return 0) instead of
+// touching memory outside the scene or the frame.
+#ifdef RLE_BOUNDS_CHECK
+__device__ unsigned int g_bounds[4];
+__device__ __forceinline__ bool in_bounds(bool ok, unsigned code, unsigned long long idx) {
+    if (!ok) {
+        const unsigned prev = atomicOr(&g_bounds[0], code);
+        if (prev == 0) {
+            g_bounds[1] = static_cast<unsigned>(idx);
+            g_bounds[2] = static_cast<unsigned>(idx >> 32);
+        }
+    }
+    return ok;
+}
+#else
+__device__ __forceinline__ bool in_bounds(bool, unsigned, unsigned long long) { return true; }
+#endif
+
 struct Counts {
     unsigned long long cells = 0, fetched = 0, headers = 0, runs = 0, spans = 0, pixels = 0;
 };
@@ -281,8 +301,9 @@ __device__ __forceinline__ Span span_setup(float res_y2, const Ray& R, float pz,
 // Fills samples y .. scr_y2-1 of a span that the occupancy mask leaves open.
 template <int G, bool kCount>
 __device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int k, uint32_t* row, float* drow,
-                                          rle_hit* hrow, const uint16_t* colours, int y, int scr_y2, const Span& sp,
-                                          int mip, int vx, int vz, Pending& pend, Counts& cnt) {
+                                          rle_hit* hrow, const uint16_t* colours, uint64_t colour_room, int S, int y,
+                                          int scr_y2, const Span& sp, int mip, int vx, int vz, Pending& pend,
+                                          Counts& cnt) {
     const float u2dz = sp.u2dz, onedz2 = sp.onedz2;
     if constexpr (kCount) cnt.spans++;
     const float mult = static_cast<float>(y + 1) - sp.scr_y1r;
@@ -307,13 +328,13 @@ __device__ __forceinline__ void draw_span(const Mask& mask, unsigned gmask, int 
         }
         const int yy = y0 + k;
         bool wrote = false;
-        if (yy < scr_y2 && !mask.get(yy)) {
+        if (yy < scr_y2 && !mask.get(yy) && in_bounds(yy < S, kBoundsRay, static_cast<unsigned long long>(yy))) {
             const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(my_uz / my_onez, umin), umax));
             const float depth = 1 / my_onez;
             const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
             pend.flush();
             pend.at = &row[yy];
-            pend.colour = __ldg(&colours[u]);
+            pend.colour = in_bounds(u < colour_room, kBoundsColour, u) ? __ldg(&colours[u]) : 0u;
             pend.z = real_z << 16;
             drow[yy] = depth;
             if (hrow) {
@@ -343,8 +364,9 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
     // clip top (:467)
     if (c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin)) return;
     if (!c.loaded) {
-        const uint2 e = __ldg(&P.table[c.mip][static_cast<size_t>(c.vx) +
-                                              static_cast<size_t>(c.vz) * (P.gridx0 >> c.mip)]);
+        const size_t ti = static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> c.mip);
+        const uint2 e = in_bounds(ti < P.table_cols[c.mip], kBoundsTable, ti) ? __ldg(&P.table[c.mip][ti])
+                                                                               : make_uint2(0u, 0u);
         c.ex = e.x;
         c.ey = e.y;
     }
@@ -358,7 +380,8 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
     float tex = 0;
     for (int r = 0; r < nruns; r++) {
         if (r > 0) {
-            sti = __ldg(&hdr[r]);
+            const uint64_t hi = static_cast<uint64_t>(c.ex) + 2u + static_cast<uint64_t>(r);
+            sti = in_bounds(hi < P.slab_words[c.mip], kBoundsHeader, hi) ? __ldg(&hdr[r]) : 0u;
             if constexpr (kCount) cnt.headers++;
         }
         int solid = static_cast<int>(sti >> 10);
@@ -398,7 +421,10 @@ __device__ __forceinline__ void merge_cell(const RayParams& P, const Ray& R, con
         const int y = mask.first_clear(scr_y1, scr_y2);
         if (y >= scr_y2) continue;
         const Span sp = span_setup(res_y2, R, c.pz, c.py, sgs, sgf, tex, texture);
-        draw_span<G, kCount>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, c.mip, c.vx, c.vz, pend, cnt);
+        const uint64_t cofs = static_cast<uint64_t>(c.ex) + 2u + static_cast<uint64_t>(nruns);
+        const uint64_t room = cofs <= P.slab_words[c.mip] ? P.slab_words[c.mip] - cofs : 0u;
+        draw_span<G, kCount>(mask, gmask, k, row, drow, hrow, colours, room, P.S, y, scr_y2, sp, c.mip, c.vx, c.vz,
+                             pend, cnt);
     }
 }
 
@@ -495,8 +521,9 @@ __device__ __forceinline__ void cell_geometry(const RayParams& P, const Ray& R, 
     const bool culled = c.pz >= 0.0f && c.pz * res_y2 + c.py <= c.pz * static_cast<float>(ymin);
     c.loaded = valid && !culled;
     if (c.loaded) {
+        const size_t ti = static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip);
         const uint2 e =
-            __ldg(&P.table[mip][static_cast<size_t>(c.vx) + static_cast<size_t>(c.vz) * (P.gridx0 >> mip)]);
+            in_bounds(ti < P.table_cols[mip], kBoundsTable, ti) ? __ldg(&P.table[mip][ti]) : make_uint2(0u, 0u);
         c.ex = e.x;
         c.ey = e.y;
     }
@@ -532,7 +559,10 @@ __device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int 
     int sg = 0, texi = 0, n = 0;
     int guard = 0x7fffffff;
     for (int r = 0; r < nruns; r++) {
-        if (r > 0) sti = __ldg(&hdr[r]);
+        if (r > 0) {
+            const uint64_t hi = static_cast<uint64_t>(c.ex) + 2u + static_cast<uint64_t>(r);
+            sti = in_bounds(hi < P.slab_words[mip], kBoundsHeader, hi) ? __ldg(&hdr[r]) : 0u;
+        }
         int solid = static_cast<int>(sti >> 10);
         sg += static_cast<int>(sti & 1023u) << mip;
         if (solid == 0) continue;
@@ -642,12 +672,15 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
             const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(uz / onez, static_cast<float>(texture)), e2.y));
             const float depth = 1 / onez;
             const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
-            pend.flush();
-            pend.at = &row[p];
-            pend.colour = __ldg(&P.slabs[mip][__float_as_uint(e3.x) + u]);
-            pend.z = real_z << 16;
-            drow[p] = depth;
-            if (hrow) {
+            const uint64_t ci = static_cast<uint64_t>(__float_as_uint(e3.x)) + u;
+            if (in_bounds(p < P.S, kBoundsRay, static_cast<unsigned long long>(p))) {
+                pend.flush();
+                pend.at = &row[p];
+                pend.colour = in_bounds(ci < P.slab_words[mip], kBoundsColour, ci) ? __ldg(&P.slabs[mip][ci]) : 0u;
+                pend.z = real_z << 16;
+                drow[p] = depth;
+            }
+            if (hrow && p < P.S) {
                 const uint32_t vxz = __float_as_uint(e3.z);
                 rle_hit h;
                 h.x = static_cast<uint16_t>(vxz & 0xffffu);
@@ -725,7 +758,10 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
             continue;
         }
         const uint16_t* colours = P.slabs[mip] + __float_as_uint(a.w);
-        draw_span<G, false>(mask, gmask, k, row, drow, hrow, colours, y, scr_y2, sp, mip, vx, vz, pend, cnt);
+        const uint64_t cofs = __float_as_uint(a.w);
+        const uint64_t room = cofs <= P.slab_words[mip] ? P.slab_words[mip] - cofs : 0u;
+        draw_span<G, false>(mask, gmask, k, row, drow, hrow, colours, room, P.S, y, scr_y2, sp, mip, vx, vz, pend,
+                            cnt);
     }
 }
 
@@ -1206,6 +1242,21 @@ rle_status launch_raycast_batch(const BatchRaycast& b, void* stream) {
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;
     }
+}
+
+bool bounds_render(unsigned* out4, bool clear) {
+#ifdef RLE_BOUNDS_CHECK
+    if (cudaMemcpyFromSymbol(out4, g_bounds, sizeof(unsigned) * 4) != cudaSuccess) return false;
+    if (clear) {
+        const unsigned z[4] = {0, 0, 0, 0};
+        if (cudaMemcpyToSymbol(g_bounds, z, sizeof(z)) != cudaSuccess) return false;
+    }
+    return true;
+#else
+    (void)out4;
+    (void)clear;
+    return false;
+#endif
 }
 
 rle_status launch_raycast(const RayParams& p, void* stream) {

@@ -18,6 +18,22 @@
 namespace rle {
 namespace {
 
+#ifdef RLE_BOUNDS_CHECK
+__device__ unsigned int g_bounds[4];
+__device__ __forceinline__ bool in_bounds(bool ok, unsigned code, unsigned long long idx) {
+    if (!ok) {
+        const unsigned prev = atomicOr(&g_bounds[0], code);
+        if (prev == 0) {
+            g_bounds[1] = static_cast<unsigned>(idx);
+            g_bounds[2] = static_cast<unsigned>(idx >> 32);
+        }
+    }
+    return ok;
+}
+#else
+__device__ __forceinline__ bool in_bounds(bool, unsigned, unsigned long long) { return true; }
+#endif
+
 __device__ __forceinline__ float step_f(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
 
 __device__ __forceinline__ int texel(float t, int size) {
@@ -71,7 +87,7 @@ __device__ __forceinline__ void resolve_pixel(const ResolveParams& P, int col, i
     const size_t pi = static_cast<size_t>(row) * P.width + col;
     // rows past the rays cast hold no data (the reference's pixel buffer
     // keeps whatever an earlier frame left there)
-    const bool cast = rr < P.rays;
+    const bool cast = rr < P.rays && in_bounds(si < static_cast<size_t>(P.rows) * P.S, kBoundsResolve, si);
     const uint32_t w = cast ? __ldg(&P.raybuf[si]) : 0u;
     const float d = cast ? __ldg(&P.raydepth[si]) : 0.0f;
     uint32_t c;
@@ -137,6 +153,21 @@ __global__ void __launch_bounds__(kResolveBlock) resolve_batch_kernel(const Batc
 
 int resolve_batch_blocks(int width, int height) {
     return static_cast<int>((static_cast<long long>(width) * height + kResolveBlock - 1) / kResolveBlock);
+}
+
+bool bounds_resolve(unsigned* out4, bool clear) {
+#ifdef RLE_BOUNDS_CHECK
+    if (cudaMemcpyFromSymbol(out4, g_bounds, sizeof(unsigned) * 4) != cudaSuccess) return false;
+    if (clear) {
+        const unsigned z[4] = {0, 0, 0, 0};
+        if (cudaMemcpyToSymbol(g_bounds, z, sizeof(z)) != cudaSuccess) return false;
+    }
+    return true;
+#else
+    (void)out4;
+    (void)clear;
+    return false;
+#endif
 }
 
 rle_status launch_resolve_batch(const BatchResolve& b, void* stream) {

@@ -44,6 +44,24 @@ struct rle_scene {
 
 namespace rle {
 
+// Zero padding after each level's slab words: keeps a column's last 16-byte
+// header group inside the allocation.  The bounds-checked build pads 64 KB,
+// so that reads its checks refuse would still land in zeros.
+#ifdef RLE_BOUNDS_CHECK
+constexpr size_t kSlabPadBytes = 65536;
+#else
+constexpr size_t kSlabPadBytes = 16;
+#endif
+
+// Bounds-check word codes (RLE_BOUNDS_CHECK builds).
+enum BoundsCode : unsigned {
+    kBoundsTable = 1u,    // column-table index past the level
+    kBoundsHeader = 2u,   // run-header index past the level's words
+    kBoundsColour = 4u,   // colour-word index past the level's words
+    kBoundsRay = 8u,      // ray-buffer row or sample index out of range
+    kBoundsResolve = 16u  // resolve fetch outside the ray buffer
+};
+
 // Host-side .rle4 parse + column-table build (no device work).
 struct HostLevel {
     int sx = 0, sy = 0, sz = 0;
@@ -77,6 +95,8 @@ struct RayParams {
     int height;                   // scene height (level 0)
     const uint2* table[RLE_MAX_MIPS];
     const uint16_t* slabs[RLE_MAX_MIPS];
+    uint64_t slab_words[RLE_MAX_MIPS];  // words per level (bounds checks)
+    uint32_t table_cols[RLE_MAX_MIPS];  // columns per level (bounds checks)
     uint32_t* raybuf;
     float* raydepth;
     rle_hit* rayhit;
@@ -149,6 +169,12 @@ rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, con
 size_t batch_capacity_words(const rle_batch* b);
 int batch_max_frames(const rle_batch* b);
 rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks);
+
+// Bounds-check words of the device code (zeros when none fired); false in
+// builds without RLE_BOUNDS_CHECK.  read: flags, first index hit; clear
+// resets them.
+bool bounds_render(unsigned* out4, bool clear);
+bool bounds_resolve(unsigned* out4, bool clear);
 
 // Scene generator pieces shared by the host and device generators.
 rle_status scenegen_check(const rle_scenegen_params* p);

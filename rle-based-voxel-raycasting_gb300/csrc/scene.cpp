@@ -251,7 +251,7 @@ extern "C" rle_status rle_scene_load_memory(const void* bytes, size_t nbytes, in
         const size_t tbytes = cols * 8;
         // 16 bytes of zero padding after the words keep 16-byte vector loads
         // of a column's last header group inside the allocation.
-        const size_t sbytes = static_cast<size_t>(hl.words) * 2 + 16;
+        const size_t sbytes = static_cast<size_t>(hl.words) * 2 + rle::kSlabPadBytes;
         if ((e = cudaMalloc(&lv.d_table, tbytes)) != cudaSuccess) { st = cuda_fail(e, "cudaMalloc(table)"); break; }
         if ((e = cudaMalloc(&lv.d_slabs, sbytes)) != cudaSuccess) { st = cuda_fail(e, "cudaMalloc(slabs)"); break; }
         if ((e = cudaMemcpy(lv.d_table, table.data(), tbytes, cudaMemcpyHostToDevice)) != cudaSuccess) { st = cuda_fail(e, "cudaMemcpy(table)"); break; }
