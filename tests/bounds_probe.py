@@ -4,7 +4,8 @@
                                           ray buffers equal the oracle's
     python tests/bounds_probe.py corrupt  a resident scene whose level-0 table
                                           points every column past the level's
-                                          words: the colour check fires
+                                          words (one visible run each): the
+                                          colour check fires
 
 Prints one line `RESULT <flags> <first index>`.  The corruption stays inside
 the checked build's 64 KB zero padding, so even an unchecked read would stay
@@ -65,17 +66,24 @@ def main(mode: str) -> int:
         info = scene.info()
         cols = info.sx[0] * info.sz[0]
         # every column: offset words-2 (its headers start at the padding),
-        # one run whose cached first header says 5 solid voxels
+        # one run whose cached first header says 5 solid voxels after 100
+        # empty ones (heights 151-155, just below the camera at 170, which
+        # looks down onto them within the level-0 distance)
         bad = np.empty(2 * cols, np.uint32)
         bad[0::2] = words - 2
-        bad[1::2] = 1 | ((5 << 10) << 16)
+        bad[1::2] = 1 | (((5 << 10) | 100) << 16)
         src = torch.from_numpy(bad.view(np.int32)).cuda()
         torch.cuda.synchronize()
         rc = _cudart().cudaMemcpy(ctypes.c_void_p(table), ctypes.c_void_p(src.data_ptr()),
                                   ctypes.c_size_t(bad.nbytes), 3)  # device to device
         assert rc == 0, rc
+        back, _ = scene.copy_level(0)
+        assert np.array_equal(back, bad), "the corrupted table did not reach the device"
         rle.render_frame(scene, cam, view, ws, ws_bytes, c, d)
         torch.cuda.synchronize()
+        col = c.cpu().numpy().view(np.uint32)
+        print(f"black {int((col == 0xff000000).sum())} sky {int((col == 0xffffccb2).sum())} "
+              f"nodata {int((col == 0).sum())} of {col.size}")
     flags, first = rle.bounds_check_read(0, clear=True)
     scene.free()
     print(f"RESULT {flags} {first}")
