@@ -415,7 +415,8 @@ def run_batched(rle, torch, scene, lv0, n_cams=64, repeats=5, seed=20261204):
                     "launches_per_batch": 2, "cuda_graph": True},
         "speedup": round(plain_ms / batch_ms, 3),
         "autotuned": {"tile_rays": best.tile_rays, "lanes_per_ray": best.lanes_per_ray, "staging": best.staging,
-                      "threads_per_block": best.threads_per_block, "tune_s": round(t_tune, 2)},
+                      "threads_per_block": best.threads_per_block, "per_frame": best.per_frame,
+                      "tune_s": round(t_tune, 2)},
     }
 
 
@@ -462,6 +463,7 @@ def run_config5(rle, torch, frames=120, views_per_batch=8, seed=7, repeats=3):
               for i in range(0, frames, views_per_batch)]
     batch = rle.Batch(max_frames=views_per_batch, raybuf_words=max(rle.batch_words_needed(g) for g in groups),
                       max_samples=4096)
+    best, _ = batch.autotune(scene, groups[0], repeats=1)
 
     def batched():
         for g in groups:
@@ -494,7 +496,9 @@ def run_config5(rle, torch, frames=120, views_per_batch=8, seed=7, repeats=3):
         "runs_per_column": round(info.run_headers / (8192 * 8192), 2),
         "plain": {"value": round(pixels / plain_ms / 1e3, 1), "unit": "Mrays/s", "ms_per_frame": round(plain_ms / frames, 4)},
         "batched": {"value": round(pixels / batch_ms / 1e3, 1), "unit": "Mrays/s",
-                    "ms_per_frame": round(batch_ms / frames, 4), "views_per_launch": views_per_batch},
+                    "ms_per_frame": round(batch_ms / frames, 4), "views_per_launch": views_per_batch,
+                    "autotuned": {"tile_rays": best.tile_rays, "lanes_per_ray": best.lanes_per_ray,
+                                  "staging": best.staging, "per_frame": best.per_frame}},
     }
     scene.free()
     return out

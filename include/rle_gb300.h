@@ -329,6 +329,8 @@ typedef struct rle_batch_tuning {
     int staging;            /* staging depth: tiles a lane group claims per grab, 1..8 */
     int threads_per_block;  /* 32, 64, 96 or 128 */
     int use_graph;          /* 1: capture once and replay (default); 0: plain launches */
+    int per_frame;          /* 1: one plain raycast + resolve launch per frame instead of the
+                               persistent pair (wins for a few large frames); 0 default */
 } rle_batch_tuning;
 
 /* max_frames per batch; raybuf_words: ray-buffer capacity shared by the
@@ -346,7 +348,8 @@ size_t rle_batch_words_needed(const rle_frame_request* frames, int n);
 rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                             void* stream);
 /* Times every tile_rays x lanes_per_ray x staging combination
- * ({1,2,4,8,16,32,64} x {8,16,32} x {1,2,3}) on these frames (median of `repeats`
+ * ({1,2,4,8,16,32,64} x {8,16,32} x {1,2,3}) and the per-frame launches (lanes
+ * {8,16,32}) on these frames (median of `repeats`
  * runs each), keeps the fastest as the batch's tuning and returns it. */
 rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                               int repeats, rle_batch_tuning* best, float* best_ms);

@@ -94,10 +94,11 @@ class FrameRequest(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("tile_rays", C.c_int), ("lanes_per_ray", C.c_int), ("staging", C.c_int),
-                ("threads_per_block", C.c_int), ("use_graph", C.c_int)]
+                ("threads_per_block", C.c_int), ("use_graph", C.c_int), ("per_frame", C.c_int)]
 
     def as_tuple(self):
-        return (self.tile_rays, self.lanes_per_ray, self.staging, self.threads_per_block, self.use_graph)
+        return (self.tile_rays, self.lanes_per_ray, self.staging, self.threads_per_block, self.use_graph,
+                self.per_frame)
 
 
 class ServerConfig(C.Structure):
@@ -442,8 +443,8 @@ class Batch:
         return t
 
     def set_tuning(self, tile_rays: int, lanes_per_ray: int, staging: int = 1, threads_per_block: int = 128,
-                   use_graph: bool = True) -> None:
-        t = BatchTuning(tile_rays, lanes_per_ray, staging, threads_per_block, int(use_graph))
+                   use_graph: bool = True, per_frame: bool = False) -> None:
+        t = BatchTuning(tile_rays, lanes_per_ray, staging, threads_per_block, int(use_graph), int(per_frame))
         _check(_lib.rle_batch_set_tuning(self.handle, C.byref(t)), "rle_batch_set_tuning")
 
     def render(self, scene: Scene, frames, stream: int = 0) -> None:

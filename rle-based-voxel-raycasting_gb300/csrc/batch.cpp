@@ -36,7 +36,8 @@ bool valid_tuning(const rle_batch_tuning& t) {
     return t.tile_rays >= 1 && t.tile_rays <= 256 && (t.lanes_per_ray == 8 || t.lanes_per_ray == 16 ||
                                                       t.lanes_per_ray == 32) &&
            t.staging >= 1 && t.staging <= 8 && t.threads_per_block >= 32 && t.threads_per_block <= 128 &&
-           t.threads_per_block % 32 == 0 && (t.use_graph == 0 || t.use_graph == 1);
+           t.threads_per_block % 32 == 0 && (t.use_graph == 0 || t.use_graph == 1) &&
+           (t.per_frame == 0 || t.per_frame == 1);
 }
 
 rle_status cuda_fail(cudaError_t e, const char* what) {
@@ -63,7 +64,7 @@ struct rle_batch {
     int parity = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    rle_batch_tuning tuning{1, 32, 1, 128, 1};
+    rle_batch_tuning tuning{1, 32, 1, 128, 1, 0};
     int raycast_blocks = 0;
     int resolve_blocks = 0;
     std::mutex mu;
@@ -219,7 +220,19 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
         st = prepare_grid(b);
         if (st != RLE_OK) return st;
     }
-    if (b->tuning.use_graph) {
+    if (b->tuning.per_frame) {
+        // one plain launch pair per frame, parameters by value from the staging block
+        const Layout& L = b->layout;
+        auto* rp = reinterpret_cast<rle::RayParams*>(b->h_params[par] + L.ray_params);
+        auto* sp = reinterpret_cast<rle::ResolveParams*>(b->h_params[par] + L.resolve_params);
+        for (int i = 0; i < n && st == RLE_OK; i++) {
+            rp[i].lanes_per_ray = b->tuning.lanes_per_ray;
+            rp[i].threads_per_block = b->tuning.threads_per_block;
+            st = rle::launch_raycast(rp[i], stream);
+            if (st == RLE_OK) st = rle::launch_resolve(sp[i], stream);
+        }
+        if (st != RLE_OK) return st;
+    } else if (b->tuning.use_graph) {
         if (!b->graph[par]) {
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
@@ -400,12 +413,15 @@ extern "C" rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, c
     rle_batch_tuning win = start;
     float win_ms = 1e30f;
     rle_status st = RLE_OK;
-    const int tiles[] = {1, 2, 4, 8, 16, 32, 64}, lanes[] = {8, 16, 32}, stagings[] = {1, 2, 3};
+    const int lanes[] = {8, 16, 32}, stagings[] = {1, 2, 3};
     for (int lv : lanes) {
-        for (int tv : tiles) {
+        // the persistent launch over tile x staging, then the per-frame launches (tile -1)
+        for (int tv : {1, 2, 4, 8, 16, 32, 64, -1}) {
             for (int sv : stagings) {
+                if (tv < 0 && sv > 1) break;
                 rle_batch_tuning t = start;
-                t.tile_rays = tv;
+                t.per_frame = tv < 0 ? 1 : 0;
+                t.tile_rays = tv < 0 ? start.tile_rays : tv;
                 t.lanes_per_ray = lv;
                 t.staging = sv;
                 if ((st = rle_batch_set_tuning(b, &t)) != RLE_OK) break;

@@ -97,7 +97,8 @@ def test_batch_matches_single_frames(rle, scene, torch_cuda):
     b.free()
 
 
-@pytest.mark.parametrize("shape", [(1, 8, 1, 128, 1), (8, 16, 3, 64, 1), (64, 32, 2, 128, 0), (16, 32, 1, 32, 1)])
+@pytest.mark.parametrize("shape", [(1, 8, 1, 128, 1, 0), (8, 16, 3, 64, 1, 0), (64, 32, 2, 128, 0, 0),
+                                   (16, 32, 1, 32, 1, 0), (1, 32, 1, 128, 1, 1), (1, 16, 1, 64, 0, 1)])
 def test_batch_shapes(rle, scene, torch_cuda, shape):
     torch = torch_cuda
     cams = _cameras(rle, scene, 7, 3)
@@ -140,6 +141,7 @@ def test_autotune_picks_a_valid_shape(rle, scene, torch_cuda):
     b = rle.Batch(max_frames=8, raybuf_words=rle.batch_words_needed(outs.reqs), max_samples=1024)
     best, ms = b.autotune(scene, outs.reqs, repeats=1)
     assert best.tile_rays in (1, 2, 4, 8, 16, 32, 64) and best.lanes_per_ray in (8, 16, 32) and best.staging in (1, 2, 3)
+    assert best.per_frame in (0, 1)
     assert ms > 0
     assert b.tuning().as_tuple() == best.as_tuple()
     b.render(scene, outs.reqs)
