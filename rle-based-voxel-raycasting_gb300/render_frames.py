@@ -1,7 +1,7 @@
 """Render frames of a seeded scene from the command line.
 
     python rle-based-voxel-raycasting_gb300/render_frames.py [--size 2048] [--height 256] [--seed 2]
-        [--width 1920] [--screen-height 1080] [--frames 6] [--fov 90] [--png-dir DIR]
+        [--width 1920] [--screen-height 1080] [--frames 6] [--fov 90] [--png-dir DIR] [--batch N]
 
 Builds the scene on the GPU (rle_scenegen_device), walks a seeded camera
 path (poses 10-80 voxels above the ground, yaw uniform, pitch up to 30
@@ -62,6 +62,8 @@ def main(argv=None) -> int:
     ap.add_argument("--frames", type=int, default=6)
     ap.add_argument("--path-seed", type=int, default=20261203)
     ap.add_argument("--png-dir", type=str, default=None)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="render the path in batches of this many frames (rle_batch, autotuned) instead")
     args = ap.parse_args(argv)
 
     import torch
@@ -89,6 +91,8 @@ def main(argv=None) -> int:
     out_dir = Path(args.png_dir) if args.png_dir else None
     if out_dir:
         out_dir.mkdir(parents=True, exist_ok=True)
+    if args.batch > 0:
+        return _batched(rle, torch, scene, info, table, words, rng, view, args)
     for i in range(args.frames):
         x, z = rng.uniform(0, info.sx[0]), rng.uniform(0, info.sz[0])
         g = rle.ground_height(table, words, info.sx[0], info.sy[0], int(x), int(z))
@@ -104,6 +108,36 @@ def main(argv=None) -> int:
         if out_dir:
             rgba = colour.cpu().numpy().view(np.uint8).reshape(H, W, 4)
             write_png(out_dir / f"frame_{i:04d}.png", np.ascontiguousarray(rgba[:, :, :3]))
+    scene.free()
+    return 0
+
+
+def _batched(rle, torch, scene, info, table, words, rng, view, args) -> int:
+    W, H = view.width, view.height
+    cams = []
+    for _ in range(args.frames):
+        x, z = rng.uniform(0, info.sx[0]), rng.uniform(0, info.sz[0])
+        g = rle.ground_height(table, words, info.sx[0], info.sy[0], int(x), int(z))
+        pitch = float(rng.uniform(1.0, 30.0) * rng.choice([-1.0, 1.0]))
+        cams.append(rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)),
+                               pitch, args.fov, scene_height=info.sy[0]))
+    outs = [(torch.empty(W * H, dtype=torch.int32, device="cuda"), torch.empty(W * H, dtype=torch.float32,
+                                                                                device="cuda"))
+            for _ in range(args.batch)]
+    groups = [[rle.frame_request(c, view, *outs[k]) for k, c in enumerate(cams[i:i + args.batch])]
+              for i in range(0, len(cams), args.batch)]
+    b = rle.Batch(args.batch, max(rle.batch_words_needed(g) for g in groups), view.samples)
+    best, ms = b.autotune(scene, groups[0], repeats=1)
+    print(f"autotuned: tile {best.tile_rays} lanes {best.lanes_per_ray} staging {best.staging} "
+          f"per_frame {best.per_frame} ({ms:.3f} ms)", flush=True)
+    for i, g in enumerate(groups):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.render(scene, g)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"batch {i}: {len(g)} frames, {e0.elapsed_time(e1):.3f} ms", flush=True)
+    b.free()
     scene.free()
     return 0
 
