@@ -64,6 +64,8 @@ def main(argv=None) -> int:
     ap.add_argument("--png-dir", type=str, default=None)
     ap.add_argument("--batch", type=int, default=0,
                     help="render the path in batches of this many frames (rle_batch, autotuned) instead")
+    ap.add_argument("--batch-lanes", type=int, default=0,
+                    help="with --batch: skip the autotuner, one-ray claims with this many lanes per ray")
     args = ap.parse_args(argv)
 
     import torch
@@ -127,9 +129,12 @@ def _batched(rle, torch, scene, info, table, words, rng, view, args) -> int:
     groups = [[rle.frame_request(c, view, *outs[k]) for k, c in enumerate(cams[i:i + args.batch])]
               for i in range(0, len(cams), args.batch)]
     b = rle.Batch(args.batch, max(rle.batch_words_needed(g) for g in groups), view.samples)
-    best, ms = b.autotune(scene, groups[0], repeats=1)
-    print(f"autotuned: tile {best.tile_rays} lanes {best.lanes_per_ray} staging {best.staging} "
-          f"per_frame {best.per_frame} ({ms:.3f} ms)", flush=True)
+    if args.batch_lanes:
+        b.set_tuning(1, args.batch_lanes, 1, 128)
+    else:
+        best, ms = b.autotune(scene, groups[0], repeats=1)
+        print(f"autotuned: tile {best.tile_rays} lanes {best.lanes_per_ray} staging {best.staging} "
+              f"per_frame {best.per_frame} ({ms:.3f} ms)", flush=True)
     for i, g in enumerate(groups):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
