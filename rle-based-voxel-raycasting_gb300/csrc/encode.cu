@@ -385,24 +385,11 @@ __device__ uint16_t normal_word(const WriteArgs& a, int x, int j, int z) {
     return static_cast<uint16_t>(ny);
 }
 
-__global__ void __launch_bounds__(kThreads) write_kernel(const __grid_constant__ WriteArgs a,
-                                                         const uint64_t* __restrict__ surf,
-                                                         const unsigned long long* __restrict__ offsets,
-                                                         const uint16_t* __restrict__ nhead,
-                                                         uint16_t* __restrict__ slabs, uint2* __restrict__ table) {
-    const long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const long long ncols = static_cast<long long>(a.sx) * a.sz;
-    if (q >= ncols) return;
-    const int x = static_cast<int>(q % a.sx), z = static_cast<int>(q / a.sx);
-    uint64_t s[kMaxWords];
-    int ncol = 0;
-    for (int w = 0; w < a.W; w++) {
-        s[w] = surf[q * a.W + w];
-        ncol += __popcll(s[w]);
-    }
-    const unsigned long long ofs = offsets[q];
-    const int nh = nhead[q];
-    uint16_t* dst = slabs + ofs;
+// One column's words -- [run count][colour count][headers][colours] -- at
+// dst (shared or global memory).  Returns the first header (valid when the
+// column has runs).
+__device__ __forceinline__ uint32_t write_column(const WriteArgs& a, const uint64_t* s, int x, int z, int nh,
+                                                 int ncol, uint16_t* dst, bool* have_first_out) {
     dst[0] = static_cast<uint16_t>(nh);
     dst[1] = static_cast<uint16_t>(ncol);
     uint16_t* hp = dst + 2;
@@ -448,6 +435,73 @@ __global__ void __launch_bounds__(kThreads) write_kernel(const __grid_constant__
         }
         end = r1;
     }
+    *have_first_out = have_first;
+    return first;
+}
+
+// u16 words a warp stages in shared memory before one coalesced copy.
+constexpr int kStageWords = 2048;
+
+// One thread per column.  The 32 columns of a warp are consecutive, so their
+// words form one contiguous range of the slab array: the lanes write their
+// columns into a shared-memory stage and the warp copies the range out with
+// 4-byte stores (2-byte ones at its two ends, which may share a word with the
+// neighbouring warps' ranges).  A warp whose range exceeds the stage writes
+// its columns directly.
+__global__ void __launch_bounds__(kThreads) write_kernel(const __grid_constant__ WriteArgs a,
+                                                         const uint64_t* __restrict__ surf,
+                                                         const unsigned long long* __restrict__ offsets,
+                                                         const uint16_t* __restrict__ nhead,
+                                                         uint16_t* __restrict__ slabs, uint2* __restrict__ table) {
+    __shared__ uint16_t stage_all[kThreads / 32][kStageWords];
+    uint16_t* stage = stage_all[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const long long q = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long long ncols = static_cast<long long>(a.sx) * a.sz;
+    const bool valid = q < ncols;
+    int x = 0, z = 0, nh = 0, ncol = 0;
+    uint64_t s[kMaxWords];
+    unsigned long long ofs = 0;
+    if (valid) {
+        x = static_cast<int>(q % a.sx);
+        z = static_cast<int>(q / a.sx);
+        for (int w = 0; w < a.W; w++) {
+            s[w] = surf[q * a.W + w];
+            ncol += __popcll(s[w]);
+        }
+        ofs = offsets[q];
+        nh = nhead[q];
+    }
+    const unsigned long long col_end = ofs + 2u + static_cast<unsigned long long>(nh + ncol);
+    // the warp's range: from lane 0's offset to the end of its last valid column
+    const unsigned valid_mask = __ballot_sync(0xffffffffu, valid);
+    if (valid_mask == 0) return;  // a warp past the level's last column
+    const int last = 31 - __clz(valid_mask);
+    const unsigned long long base = __shfl_sync(0xffffffffu, ofs, 0);
+    const unsigned long long stop = __shfl_sync(0xffffffffu, col_end, last);
+    const bool staged = stop - base <= static_cast<unsigned long long>(kStageWords);
+    bool have_first = false;
+    uint32_t first = 0;
+    if (valid) {
+        uint16_t* dst = staged ? stage + (ofs - base) : slabs + ofs;
+        first = write_column(a, s, x, z, nh, ncol, dst, &have_first);
+    }
+    if (staged) {
+        __syncwarp();
+        const int n = static_cast<int>(stop - base);
+        uint16_t* g = slabs + base;
+        int start = 0;
+        if ((reinterpret_cast<uintptr_t>(g) & 2u) && n > 0) {
+            if (lane == 0) g[0] = stage[0];
+            start = 1;
+        }
+        const int pairs = (n - start) >> 1;
+        uint32_t* g32 = reinterpret_cast<uint32_t*>(g + start);
+        for (int i = lane; i < pairs; i += 32)
+            g32[i] = static_cast<uint32_t>(stage[start + 2 * i]) | (static_cast<uint32_t>(stage[start + 2 * i + 1]) << 16);
+        if (((n - start) & 1) && lane == 0) g[n - 1] = stage[n - 1];
+    }
+    if (!valid) return;
     // RLE4::load's table entry (src/Rle4.cpp:285-314): the word after the
     // two counts is read as the first header even for an empty column, where
     // it is the next column's run count (or nothing past the level's end).
