@@ -20,6 +20,7 @@ Render::render_line + the resolve, all host threads) on the same frames.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import math
 import os
@@ -109,6 +110,7 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            atexit.register(self.__exit__, None, None, None)  # never leave the sampler running
         except (OSError, ValueError):
             self.proc = None
         return self
@@ -118,7 +120,7 @@ class ClockSampler:
             self.lines.append(ln.strip())
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -142,6 +144,17 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def clock_summary(primary: ClockSampler, whole: ClockSampler) -> dict:
+    """Median SM clock and throttle reasons over the whole GPU run, with the
+    samples that fell inside the plain-frame timed region beside them."""
+    a, b = primary.summary(), whole.summary()
+    out = dict(b) if b["samples"] else dict(a)
+    out["reasons"] = sorted(set(a["reasons"]) | set(b["reasons"]))
+    out["window"] = "warm-up to the last config-5 frame, nvidia-smi every 200 ms"
+    out["timed_region"] = a
+    return out
 
 
 def measured_peak_hbm():
@@ -204,6 +217,9 @@ def run_ours(args):
     def step(i):
         rle.render_frame(scene, cams[i], view, ws, ws_bytes, colour, depth, None, stream=sp)
 
+    # clocks over every GPU section of the run (warm-up to the config-5 frames):
+    # the plain-frame region alone is shorter than nvidia-smi's sampling period
+    clk_all = ClockSampler(local).__enter__()
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
             step(i)
@@ -292,6 +308,7 @@ def run_ours(args):
     config5 = None
     if args.config5_frames > 0:
         config5 = run_config5(rle, torch, frames=args.config5_frames)
+    clk_all.__exit__(None, None, None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -332,7 +349,7 @@ def run_ours(args):
                                        "(profiles/raycast_1080p_cave2048.md)",
                      "kernel": "raycast_kernel", "kernel_ms": round(k_ms, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": int(sum(algo_bytes) / len(algo_bytes))},
-        "clocks": clk.summary(),
+        "clocks": clock_summary(clk, clk_all),
         "wall_s_timed": round(t_wall, 3),
     }
     if cpu:

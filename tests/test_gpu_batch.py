@@ -112,6 +112,24 @@ def test_batch_shapes(rle, scene, torch_cuda, shape):
     b.free()
 
 
+@pytest.mark.parametrize("lanes", [8, 16, 32])
+def test_batch_maximum_samples(rle, scene, torch_cuda, lanes):
+    """A batch created for 16384 samples per ray (the library's limit) mixing
+    frames at that row length with ordinary ones equals the plain launches."""
+    torch = torch_cuda
+    cams = []
+    for i, (cam, view) in enumerate(_cameras(rle, scene, 4, 9)):
+        if i % 2 == 0:
+            view = rle.view_params(320, 240, samples=16384, maxres=48, mip_distance=96)
+        cams.append((cam, view))
+    outs = Outputs(torch, rle, cams)
+    b = rle.Batch(max_frames=4, raybuf_words=rle.batch_words_needed(outs.reqs), max_samples=16384, with_hits=True)
+    b.set_tuning(1, lanes, 1, 128)
+    b.render(scene, outs.reqs)
+    _check(rle, torch, scene, cams, outs, f"S=16384, {lanes} lanes")
+    b.free()
+
+
 def test_batch_refuses_what_it_cannot_hold(rle, scene, torch_cuda):
     torch = torch_cuda
     cams = _cameras(rle, scene, 3, 4)

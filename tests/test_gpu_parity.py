@@ -153,6 +153,34 @@ def test_random_poses_many(rle, po, caves256, torch_cuda):
     assert total > 0
 
 
+@pytest.mark.parametrize("pose", [(30.0, -8.0, 20.0), (215.0, -60.0, 90.0)])
+def test_maximum_samples(rle, po, caves256, torch_cuda, pose):
+    """16384 samples per column ray (the largest ray buffer row the library
+    accepts): a 514-word occupancy mask per ray, rows far beyond the packed
+    short-span path; counting and fast launches and the resolve."""
+    scene, oscene, _ = caves256
+    yaw, pitch, above = pose
+    t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
+    x, z = 140.5, 60.75
+    ground = rle.ground_height(t0, s0, 256, 256, int(x), int(z))
+    cam = rle.camera(x, z, ground + above, yaw, pitch)
+    rm = rle.raymap_build(cam, rle.view_params(400, 300, samples=16384, maxres=64, mip_distance=128))
+    assert rm.samples == 16384 and rm.rays > 0
+    orc, om = _oracle_frame(po, rm, oscene)
+    fr = Frame(torch_cuda, rle, scene, rm)
+    gpu = fr.rays_host()
+    assert_rays_equal(gpu, orc, f"S=16384 {pose}")
+    assert counters_dict(gpu[3]) == oracle_counters(orc[3])
+    fast = Frame(torch_cuda, rle, scene, rm, hits=True, counters=False).rays_host()
+    assert_rays_equal(fast, orc, f"S=16384 {pose} (no counters)")
+    col, dep, hit = fr.resolve_host()
+    ocol, odep, ohit, _ = po.resolve(om, 400, 300, orc[0], orc[1], orc[2])
+    assert np.array_equal(col, ocol) and np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
+    assert np.array_equal(hit, ohit)
+    with pytest.raises(rle.RLEError):
+        rle.raymap_build(cam, rle.view_params(400, 300, samples=16385))
+
+
 def test_config2_scene_frames(rle, po, torch_cuda):
     """The benchmark's scene (2048^2 x 256 caves, seed 2) and camera law at
     960x540: the fast path (early ray termination, no counters) against the
