@@ -436,44 +436,24 @@ struct Walk {
     int mapswitch, mip;
 };
 
-// One DDA step (:376-414).  Uniform groups (G == 32: one ray per warp) take
-// the branch; smaller groups use selects so rays sharing a warp do not diverge.
-template <bool kBranch>
+// One DDA step (:376-414), written with selects: the chain from one step to
+// the next is a compare and a select (the additions for both axes are issued
+// beside the compare), shorter than a branch on the compare.
 __device__ __forceinline__ void dda_step(Dda& d) {
-    if (kBranch) {
-        if (d.dd1 < d.dd0) {
-            d.dd_now = d.dd1;
-            d.index = 1;
-            d.dd1 += d.gd1;
-            d.pnx = d.i1x;
-            d.pny = d.i1y;
-            d.i1x += d.g1x;
-            d.i1y += d.g1y;
-        } else {
-            d.dd_now = d.dd0;
-            d.index = 0;
-            d.pnx = d.i0x;
-            d.pny = d.i0y;
-            d.dd0 += d.gd0;
-            d.i0x += d.g0x;
-            d.i0y += d.g0y;
-        }
-    } else {
-        const bool c1 = d.dd1 < d.dd0;
-        d.dd_now = c1 ? d.dd1 : d.dd0;
-        d.index = c1 ? 1 : 0;
-        d.pnx = c1 ? d.i1x : d.i0x;
-        d.pny = c1 ? d.i1y : d.i0y;
-        const float n1 = d.dd1 + d.gd1, n0 = d.dd0 + d.gd0;
-        const float a1x = d.i1x + d.g1x, a1y = d.i1y + d.g1y;
-        const float a0x = d.i0x + d.g0x, a0y = d.i0y + d.g0y;
-        d.dd1 = c1 ? n1 : d.dd1;
-        d.i1x = c1 ? a1x : d.i1x;
-        d.i1y = c1 ? a1y : d.i1y;
-        d.dd0 = c1 ? d.dd0 : n0;
-        d.i0x = c1 ? d.i0x : a0x;
-        d.i0y = c1 ? d.i0y : a0y;
-    }
+    const bool c1 = d.dd1 < d.dd0;
+    d.dd_now = c1 ? d.dd1 : d.dd0;
+    d.index = c1 ? 1 : 0;
+    d.pnx = c1 ? d.i1x : d.i0x;
+    d.pny = c1 ? d.i1y : d.i0y;
+    const float n1 = d.dd1 + d.gd1, n0 = d.dd0 + d.gd0;
+    const float a1x = d.i1x + d.g1x, a1y = d.i1y + d.g1y;
+    const float a0x = d.i0x + d.g0x, a0y = d.i0y + d.g0y;
+    d.dd1 = c1 ? n1 : d.dd1;
+    d.i1x = c1 ? a1x : d.i1x;
+    d.i1y = c1 ? a1y : d.i1y;
+    d.dd0 = c1 ? d.dd0 : n0;
+    d.i0x = c1 ? d.i0x : a0x;
+    d.i0y = c1 ? d.i0y : a0y;
 }
 
 // Level-of-detail switch at the top of a step (:343-365): past the switch
@@ -789,11 +769,13 @@ __device__ __forceinline__ int dda_chunk(const RayParams& P, Walk& W, int k, uns
     // floats: when neither a LOD switch nor the end of the ray can
     // fall inside the chunk, the steps need no checks
     const int zi = static_cast<int>(W.z), dzi = static_cast<int>(W.dz);
-    const bool plain = W.mapswitch >= zi && (W.mapswitch - zi) / dzi + 1 >= G && (P.z_far - zi) / dzi >= G;
+    // every step's z stays at or below the switch distance and the chunk's
+    // last z at or below z_far (dz > 0; the products stay far below 2^31)
+    const bool plain = W.mapswitch - zi >= (G - 1) * dzi && P.z_far - zi >= G * dzi;
     if (plain) {
 #pragma unroll
         for (int s = 0; s < G; s++) {
-            dda_step<G == 32>(W.d);
+            dda_step(W.d);
             if (s == k) {
                 c_dd = W.d.dd_now;
                 c_px = W.d.pnx;
@@ -816,7 +798,7 @@ __device__ __forceinline__ int dda_chunk(const RayParams& P, Walk& W, int k, uns
                 ended_here = true;
                 break;
             }
-            dda_step<G == 32>(W.d);
+            dda_step(W.d);
             if (s == k) {
                 c_dd = W.d.dd_now;
                 c_px = W.d.pnx;
@@ -936,6 +918,10 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             const bool ended = nvalid < G;
             const bool valid = k < nvalid;
             const float t_end = W.d.dd_now;  // DDA distance at the end of this chunk
+            // whether the ray can end after this chunk, tested at the horizon
+            // before the merge: ymin only grows, so a test that passes now
+            // passes after the merge too, and its latency hides under the DDA
+            const bool done_next = !kCount && ray_is_done(P, R, t_end, ymin);
             // ---- 1. the next chunk's DDA steps and column-table fetches are
             // issued now; their loads complete while this chunk is merged ----
             int nvalid_next = 0;
@@ -1009,7 +995,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             // every later cell projects below the floating horizon (the
             // reference walks on to z_far without drawing).  Exact counters
             // need the full walk, so they keep it.
-            if (!kCount && ray_is_done(P, R, t_end, ymin)) break;
+            if (done_next) break;
             c = c_next;
             nvalid = nvalid_next;
         }
