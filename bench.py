@@ -55,7 +55,9 @@ def load_rle():
 # DRAM bytes of one raycast launch on this workload, from the ncu capture
 # summarised in profiles/raycast_1080p_cave2048.md (a profiler run cannot be
 # part of the timed benchmark; the capture is repeated when the kernel changes).
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 22_368_256
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 22_526_464
+# frames in flight in the end-to-end loop (one stream, workspace and output set each)
+E2E_FRAMES_IN_FLIGHT = 3
 
 
 def pow2_ceil(v: int) -> int:
@@ -272,28 +274,31 @@ def run_ours(args):
     peak, peak_kind = measured_peak_hbm()
 
     # ---- end to end: camera from host through the C ABI, colour + depth of
-    # every frame back to pinned host memory; frames alternate between two
-    # streams (own workspace and outputs each) so one frame's read-back
-    # overlaps the next frame's render, as a renderer's frame loop does ----
-    stream2 = torch.cuda.Stream()
-    sets = [(stream, ws, colour, depth), (stream2, torch.empty_like(ws), torch.empty_like(colour),
-                                          torch.empty_like(depth))]
+    # every frame back to pinned host memory; a triple-buffered frame loop:
+    # frames rotate over E2E_FRAMES_IN_FLIGHT streams (own workspace and
+    # outputs each), so a frame's read-back and its last rays overlap the
+    # next frames' renders ----
+    sets = [(stream, ws, colour, depth)]
+    for _ in range(E2E_FRAMES_IN_FLIGHT - 1):
+        sets.append((torch.cuda.Stream(), torch.empty_like(ws), torch.empty_like(colour), torch.empty_like(depth)))
     hosts = [(torch.empty(W * H, dtype=torch.int32, pin_memory=True),
-              torch.empty(W * H, dtype=torch.float32, pin_memory=True)) for _ in range(2)]
+              torch.empty(W * H, dtype=torch.float32, pin_memory=True)) for _ in sets]
     torch.cuda.synchronize()
-    e0, e1, ej = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-                  torch.cuda.Event())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    stream2.wait_event(e0)
+    for s_ in sets[1:]:
+        s_[0].wait_event(e0)
     for k in range(args.steps):
-        s_, w_, c_, d_ = sets[k % 2]
-        hc, hd = hosts[k % 2]
+        s_, w_, c_, d_ = sets[k % len(sets)]
+        hc, hd = hosts[k % len(sets)]
         with torch.cuda.stream(s_):
             rle.render_frame(scene, cams[args.warmup + k], view, w_, ws_bytes, c_, d_, None, stream=s_.cuda_stream)
             hc.copy_(c_, non_blocking=True)
             hd.copy_(d_, non_blocking=True)
-    ej.record(stream2)
-    stream.wait_event(ej)
+    for s_ in sets[1:]:
+        ej = torch.cuda.Event()
+        ej.record(s_[0])
+        stream.wait_event(ej)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
@@ -340,7 +345,7 @@ def run_ours(args):
         },
         "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 28,
                 "d2h_bytes_per_step": W * H * 8,
-                "pipeline": "frames alternate between 2 streams; a frame's read-back and tail overlap the next render",
+                "pipeline": f"triple-buffered frame loop: frames rotate over {E2E_FRAMES_IN_FLIGHT} streams; a frame's read-back and last rays overlap the next frames' renders",
                 "l2": "not flushed: the scene (294 MB) exceeds L2 and every frame has its own camera"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
