@@ -250,7 +250,7 @@ struct Cell {
 
 // Candidate runs a lane records per cell for the merge (shared memory,
 // 3 x float4 per run).
-constexpr int kRecs = 4;
+constexpr int kRecs = 7;
 
 // A lane's last coloured sample, stored one pass late: the colour gather
 // (a dependent load) then overlaps the following work instead of stalling
