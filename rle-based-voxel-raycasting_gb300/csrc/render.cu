@@ -250,7 +250,7 @@ struct Cell {
 
 // Candidate runs a lane records per cell for the merge (shared memory,
 // 3 x float4 per run).
-constexpr int kRecs = 7;
+constexpr int kRecs = 8;
 
 // A lane's last coloured sample, stored one pass late: the colour gather
 // (a dependent load) then overlaps the following work instead of stalling
@@ -592,7 +592,15 @@ __device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int 
 // sample per lane.  A span of at most kShortSpan samples lies in two mask
 // words, and a sample m places into its span needs m accumulation steps,
 // which the lane replays from the span's start.  Longer spans are filled at
-// once by draw_span.  Queue entry: 4 x float4 in shared memory.
+// once by draw_span.  Queue entry: 3 x float4 in shared memory,
+//   {first free sample | level << 16, claimed bits of the span's two mask
+//    words, colour offset of the column},
+//   {scr_y1r, u1z, u2dz, onez1},
+//   {onedz2, texture | colours of the run << 16, sg0, vx | vz << 16}
+// (the sample index is below 2^14, a column holds fewer than 2^16 colours
+// and a run at most 63, so the fields fit; the clamp bound umax is the
+// float of texture + colours - 1, exactly as the walk computes it).
+constexpr int kQueueVecs = 3;
 constexpr int kShortSpan = 32;
 
 struct SpanQueue {
@@ -608,8 +616,8 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
     // samples per queued span, inclusive prefix over the group's lanes
     int cnt = 0;
     if (k < q.n) {
-        const float4 e0 = q.e[4 * k];
-        cnt = __popc(__float_as_uint(e0.z)) + __popc(__float_as_uint(e0.w));
+        const float4 e0 = q.e[kQueueVecs * k];
+        cnt = __popc(__float_as_uint(e0.y)) + __popc(__float_as_uint(e0.z));
     }
     int incl = cnt;
 #pragma unroll
@@ -633,12 +641,13 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
         }
         const int before = __shfl_sync(gmask, incl - cnt, lb + lo);
         if (t < total) {
-            const float4 e0 = q.e[4 * lo], e1 = q.e[4 * lo + 1], e2 = q.e[4 * lo + 2], e3 = q.e[4 * lo + 3];
-            const uint32_t own0 = __float_as_uint(e0.z), own1 = __float_as_uint(e0.w);
+            const float4 e0 = q.e[kQueueVecs * lo], e1 = q.e[kQueueVecs * lo + 1], e2 = q.e[kQueueVecs * lo + 2];
+            const uint32_t own0 = __float_as_uint(e0.y), own1 = __float_as_uint(e0.z);
             const int r = t - before, c0 = __popc(own0);
             const int bit = r < c0 ? static_cast<int>(__fns(own0, 0, r + 1)) : 32 + static_cast<int>(__fns(own1, 0, r - c0 + 1));
-            const int y = __float_as_int(e0.x);
-            const int p = __float_as_int(e0.y) + bit;  // base + bit
+            const int y = static_cast<int>(__float_as_uint(e0.x) & 0xffffu);
+            const int mip = static_cast<int>(__float_as_uint(e0.x) >> 16);
+            const int p = (y & ~31) + bit;  // the span's first mask word + bit
             const float u2dz = e1.z, onedz2 = e2.x;
             const float mult = static_cast<float>(y + 1) - e1.x;
             float uz = e1.y + u2dz * mult;
@@ -647,12 +656,12 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
                 uz += u2dz;
                 onez += onedz2;
             }
-            const int texture = __float_as_int(e2.z);
-            const int mip = __float_as_int(e3.y);
-            const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(uz / onez, static_cast<float>(texture)), e2.y));
+            const int texture = static_cast<int>(__float_as_uint(e2.y) & 0xffffu);
+            const float umax = static_cast<float>(texture + static_cast<int>(__float_as_uint(e2.y) >> 16) - 1);
+            const uint32_t u = static_cast<uint32_t>(fminf(fmaxf(uz / onez, static_cast<float>(texture)), umax));
             const float depth = 1 / onez;
             const uint32_t real_z = static_cast<uint32_t>(static_cast<int>(depth) & 0xfffe);
-            const uint64_t ci = static_cast<uint64_t>(__float_as_uint(e3.x)) + u;
+            const uint64_t ci = static_cast<uint64_t>(__float_as_uint(e0.w)) + u;
             if (in_bounds(p < P.S, kBoundsRay, static_cast<unsigned long long>(p))) {
                 pend.flush();
                 pend.at = &row[p];
@@ -661,11 +670,11 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
                 drow[p] = depth;
             }
             if (hrow && p < P.S) {
-                const uint32_t vxz = __float_as_uint(e3.z);
+                const uint32_t vxz = __float_as_uint(e2.w);
                 rle_hit h;
                 h.x = static_cast<uint16_t>(vxz & 0xffffu);
                 h.z = static_cast<uint16_t>(vxz >> 16);
-                h.y = static_cast<uint16_t>((__float_as_int(e2.w) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
+                h.y = static_cast<uint16_t>((__float_as_int(e2.z) >> mip) + static_cast<int>(u - static_cast<uint32_t>(texture)));
                 h.mip = static_cast<uint8_t>(mip);
                 h.flags = 1;
                 hrow[p] = h;
@@ -726,12 +735,14 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
             if (k == 0) {
                 mask.w[wi] = m0 | r0;
                 if (r1) mask.w[wi + 1] = m1 | r1;
-                float4* e = q.e + 4 * q.n;
-                e[0] = make_float4(__int_as_float(y), __int_as_float(base), __uint_as_float(own0), __uint_as_float(own1));
+                float4* e = q.e + kQueueVecs * q.n;
+                const int colours_in_run = static_cast<int>(d.y) + 1 - sp.texture;  // d.y = texture + colours - 1
+                e[0] = make_float4(__uint_as_float(static_cast<uint32_t>(y) | (static_cast<uint32_t>(mip) << 16)),
+                                   __uint_as_float(own0), __uint_as_float(own1), a.w);
                 e[1] = b;
-                e[2] = d;
-                e[3] = make_float4(__uint_as_float(__float_as_uint(a.w)), __int_as_float(mip),
-                                   __uint_as_float(static_cast<uint32_t>(vx) | (static_cast<uint32_t>(vz) << 16)), 0.0f);
+                e[2] = make_float4(d.x, __uint_as_float(static_cast<uint32_t>(sp.texture) |
+                                                        (static_cast<uint32_t>(colours_in_run) << 16)),
+                                   d.w, __uint_as_float(static_cast<uint32_t>(vx) | (static_cast<uint32_t>(vz) << 16)));
             }
             __syncwarp(gmask);
             q.n++;
@@ -1032,11 +1043,13 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
 __host__ __device__ __forceinline__ int mask_region_words(int slots, int words) {
     return (slots * words + 3) & ~3;
 }
-__host__ __device__ __forceinline__ size_t raycast_smem_bytes(int threads, int slots, int words) {
-    // masks | run records (kRecs per thread) | span queues (32 / slots-per-warp entries per ray,
-    // i.e. one per lane of the group: as many entries per block as threads)
+__host__ __device__ __forceinline__ size_t raycast_smem_bytes(int threads, int slots, int words, bool queues) {
+    // masks | run records (kRecs per thread) | span queues, in the variants that
+    // defer short spans (32 / slots-per-warp entries per ray, i.e. one per
+    // lane of the group: as many entries per block as threads)
     return static_cast<size_t>(mask_region_words(slots, words)) * 4 +
-           static_cast<size_t>(threads) * kRecs * 3 * sizeof(float4) + static_cast<size_t>(threads) * 4 * sizeof(float4);
+           static_cast<size_t>(threads) * kRecs * 3 * sizeof(float4) +
+           (queues ? static_cast<size_t>(threads) * kQueueVecs * sizeof(float4) : 0u);
 }
 
 // Lane layout of a group of G lanes within a block.
@@ -1064,7 +1077,9 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
     const int x = blockIdx.x * rays_per_block + L.slot;
     const int words = (P.S + 31) >> 5;
     float4* recs = reinterpret_cast<float4*>(smem + mask_region_words(rays_per_block, words));
-    float4* spans = recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (4 * G);
+    float4* spans =
+        kDefer ? recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (kQueueVecs * G)
+               : nullptr;
     Counts cnt;
     cast_ray<G, kCount, kHits, kDefer>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, cnt);
 }
@@ -1084,7 +1099,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
     uint32_t* mask_words = smem + L.slot * max_words;
     float4* recs = reinterpret_cast<float4*>(
         smem + mask_region_words((static_cast<int>(blockDim.x) >> 5) * (32 / G), max_words));
-    float4* spans = recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (4 * G);
+    float4* spans = nullptr;  // no deferred spans in the batched launch
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
     // Guided self-scheduling: a group claims up to tile * staging rays, but
@@ -1123,7 +1138,7 @@ template <int G, bool kCount, bool kHits, bool kDefer>
 rle_status launch_variant(const RayParams& p, int threads, cudaStream_t stream) {
     const int words = (p.S + 31) >> 5;
     const int rays_per_block = threads / 32 * (32 / G);
-    const size_t smem = raycast_smem_bytes(threads, rays_per_block, words);
+    const size_t smem = raycast_smem_bytes(threads, rays_per_block, words, kDefer);
     if (smem > 227 * 1024) {
         set_error("rle_render_rays: %d samples per ray exceed shared memory at this launch shape", p.S);
         return RLE_ERR_CAPACITY;
@@ -1162,7 +1177,7 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
 
 template <int G>
 size_t batch_smem(int threads, int max_samples) {
-    return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5);
+    return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5, false);
 }
 
 template <int G, bool kHits>
