@@ -603,6 +603,11 @@ __device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int 
 constexpr int kQueueVecs = 3;
 constexpr int kShortSpan = 32;
 
+// The packed fill of short spans pays at up to 2048 samples per ray (1080p
+// frames -2%, 480p -5%, batches of up to 1080p -3%); at 4096 it costs more
+// than it saves (4K frames +4%, batches of 4K frames +17%).
+constexpr int kDeferMaxSamples = 2048;
+
 struct SpanQueue {
     float4* e;  // G entries of this ray
     int n;
@@ -1088,7 +1093,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
 // index space (ray_start[f] = first global ray of frame f); each group takes
 // `tile` consecutive rays at a time from a global counter until none are
 // left, so long and short rays of every frame balance across the GPU.
-template <int G, bool kHits>
+template <int G, bool kHits, bool kDefer>
 __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, const int* __restrict__ ray_start,
                                                             const RayParams* __restrict__ frames, int tile,
                                                             int staging, int max_words) {
@@ -1099,7 +1104,9 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
     uint32_t* mask_words = smem + L.slot * max_words;
     float4* recs = reinterpret_cast<float4*>(
         smem + mask_region_words((static_cast<int>(blockDim.x) >> 5) * (32 / G), max_words));
-    float4* spans = nullptr;  // no deferred spans in the batched launch
+    float4* spans =
+        kDefer ? recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (kQueueVecs * G)
+               : nullptr;
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
     // Guided self-scheduling: a group claims up to tile * staging rays, but
@@ -1128,7 +1135,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 }
                 f = lo;
             }
-            cast_ray<G, false, kHits, false>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k, L.gmask,
+            cast_ray<G, false, kHits, kDefer>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k, L.gmask,
                                              cnt);
         }
     }
@@ -1165,9 +1172,7 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
         return p.rayhit ? launch_variant<G, true, true, false>(p, threads, stream)
                         : launch_variant<G, true, false, false>(p, threads, stream);
     }
-    // the packed fill of short spans pays at up to 2048 samples per ray
-    // (1080p: -2%, 480p: -5%); at 4096 it costs more than it saves
-    if (p.S <= 2048) {
+    if (p.S <= kDeferMaxSamples) {
         return p.rayhit ? launch_variant<G, false, true, true>(p, threads, stream)
                         : launch_variant<G, false, false, true>(p, threads, stream);
     }
@@ -1175,25 +1180,26 @@ rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
                     : launch_variant<G, false, false, false>(p, threads, stream);
 }
 
-template <int G>
+template <int G, bool kDefer>
 size_t batch_smem(int threads, int max_samples) {
-    return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5, false);
+    return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5, kDefer);
 }
 
-template <int G, bool kHits>
+template <int G, bool kHits, bool kDefer>
 rle_status batch_blocks(int threads, int max_samples, int* blocks) {
-    const size_t smem = batch_smem<G>(threads, max_samples);
+    const size_t smem = batch_smem<G, kDefer>(threads, max_samples);
     if (smem > 227 * 1024) {
         set_error("batch: %d samples per ray exceed shared memory at this launch shape", max_samples);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G, kHits>,
+    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G, kHits, kDefer>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int dev = 0, sms = 0, per_sm = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G, kHits>, threads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G, kHits, kDefer>, threads,
+                                                          smem);
     if (e != cudaSuccess) {
         set_error("batch launch set-up: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
@@ -1202,16 +1208,16 @@ rle_status batch_blocks(int threads, int max_samples, int* blocks) {
     return RLE_OK;
 }
 
-template <int G, bool kHits>
+template <int G, bool kHits, bool kDefer>
 rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
-    const size_t smem = batch_smem<G>(b.threads, b.max_samples);
+    const size_t smem = batch_smem<G, kDefer>(b.threads, b.max_samples);
     int blocks = b.blocks;
     if (blocks <= 0) {
-        const rle_status st = batch_blocks<G, kHits>(b.threads, b.max_samples, &blocks);
+        const rle_status st = batch_blocks<G, kHits, kDefer>(b.threads, b.max_samples, &blocks);
         if (st != RLE_OK) return st;
     }
-    raycast_batch_kernel<G, kHits><<<blocks, b.threads, smem, stream>>>(b.header, b.ray_start, b.frames, b.tile,
-                                                                        b.staging, (b.max_samples + 31) >> 5);
+    raycast_batch_kernel<G, kHits, kDefer><<<blocks, b.threads, smem, stream>>>(
+        b.header, b.ray_start, b.frames, b.tile, b.staging, (b.max_samples + 31) >> 5);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("batch raycast launch: %s", cudaGetErrorString(e));
@@ -1220,16 +1226,28 @@ rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
     return RLE_OK;
 }
 
+template <int G, bool kDefer>
+rle_status batch_blocks_for(int threads, int max_samples, bool hits, int* blocks) {
+    return hits ? batch_blocks<G, true, kDefer>(threads, max_samples, blocks)
+                : batch_blocks<G, false, kDefer>(threads, max_samples, blocks);
+}
+
+template <int G, bool kDefer>
+rle_status batch_launch_for(const BatchRaycast& b, cudaStream_t s) {
+    return b.hits ? batch_launch<G, true, kDefer>(b, s) : batch_launch<G, false, kDefer>(b, s);
+}
+
 }  // namespace
 
 rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks) {
+    const bool defer = max_samples <= kDeferMaxSamples;
     switch (lanes) {
-        case 8: return hits ? batch_blocks<8, true>(threads, max_samples, blocks)
-                            : batch_blocks<8, false>(threads, max_samples, blocks);
-        case 16: return hits ? batch_blocks<16, true>(threads, max_samples, blocks)
-                             : batch_blocks<16, false>(threads, max_samples, blocks);
-        case 32: return hits ? batch_blocks<32, true>(threads, max_samples, blocks)
-                             : batch_blocks<32, false>(threads, max_samples, blocks);
+        case 8: return defer ? batch_blocks_for<8, true>(threads, max_samples, hits, blocks)
+                             : batch_blocks_for<8, false>(threads, max_samples, hits, blocks);
+        case 16: return defer ? batch_blocks_for<16, true>(threads, max_samples, hits, blocks)
+                              : batch_blocks_for<16, false>(threads, max_samples, hits, blocks);
+        case 32: return defer ? batch_blocks_for<32, true>(threads, max_samples, hits, blocks)
+                              : batch_blocks_for<32, false>(threads, max_samples, hits, blocks);
         default:
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;
@@ -1242,10 +1260,11 @@ rle_status launch_raycast_batch(const BatchRaycast& b, void* stream) {
         return RLE_ERR_INVALID_ARG;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const bool defer = b.max_samples <= kDeferMaxSamples;
     switch (b.lanes) {
-        case 8: return b.hits ? batch_launch<8, true>(b, s) : batch_launch<8, false>(b, s);
-        case 16: return b.hits ? batch_launch<16, true>(b, s) : batch_launch<16, false>(b, s);
-        case 32: return b.hits ? batch_launch<32, true>(b, s) : batch_launch<32, false>(b, s);
+        case 8: return defer ? batch_launch_for<8, true>(b, s) : batch_launch_for<8, false>(b, s);
+        case 16: return defer ? batch_launch_for<16, true>(b, s) : batch_launch_for<16, false>(b, s);
+        case 32: return defer ? batch_launch_for<32, true>(b, s) : batch_launch_for<32, false>(b, s);
         default:
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;
