@@ -21,6 +21,7 @@ from __future__ import annotations
 
 import argparse
 import atexit
+import gc
 import json
 import math
 import os
@@ -577,15 +578,23 @@ def run_serving(rle, torch, seconds=5.0, lam=2000.0, seed=20261205, scenes=None)
         entry = {}
         for load in ("offered", "offered_2x", "saturated"):
             srv.reset_stats()
+            # the submitting thread is the load generator: a full collection
+            # of the interpreter's objects (tens of ms) would hold back the
+            # arrivals behind it and release them as one burst
+            gc.collect()
+            gc.disable()
             t0 = time.perf_counter()
             rate = {"offered": 1.0, "offered_2x": 2.0}.get(load)
-            for i, (sid, cam, v) in enumerate(reqs):
-                if rate:
-                    delay = t0 + arrivals[i] / rate - time.perf_counter()
-                    if delay > 0:
-                        time.sleep(delay)
-                c, d = outs[i % ring]
-                srv.submit(sid, cam, v, c, d)
+            try:
+                for i, (sid, cam, v) in enumerate(reqs):
+                    if rate:
+                        delay = t0 + arrivals[i] / rate - time.perf_counter()
+                        if delay > 0:
+                            time.sleep(delay)
+                    c, d = outs[i % ring]
+                    srv.submit(sid, cam, v, c, d)
+            finally:
+                gc.enable()
             srv.drain(600000)
             srv.poll(1 << 20)
             st = srv.stats()
