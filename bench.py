@@ -56,7 +56,7 @@ def load_rle():
 # DRAM bytes of one raycast launch on this workload, from the ncu capture
 # summarised in profiles/raycast_1080p_cave2048.md (a profiler run cannot be
 # part of the timed benchmark; the capture is repeated when the kernel changes).
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 22_291_200
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 22_462_720
 # frames in flight in the end-to-end loop (one stream, workspace and output set each)
 E2E_FRAMES_IN_FLIGHT = 3
 
