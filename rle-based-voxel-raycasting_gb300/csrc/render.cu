@@ -9,16 +9,21 @@
 // an occupancy bitmask.
 //
 // Parallel decomposition: a group of G lanes (G = 8, 16 or 32; 32/G rays
-// per warp) owns one ray.  The ray is processed in chunks of G DDA steps:
-//   1. lane k replays the DDA from the chunk start for k steps and takes
-//      step k (the DDA is a chain of IEEE additions, so every lane repeats
-//      the same operations); the last lane's state starts the next chunk;
+// per warp) owns one ray.  The ray is processed in chunks of G DDA steps,
+// the next chunk's DDA and table fetches issued before this chunk's merge:
+//   1. all lanes step the DDA in lockstep (the DDA is a chain of IEEE
+//      additions, so every lane repeats the same operations) and lane k
+//      keeps the state of step k; the state before it comes from lane k-1;
 //   2. each lane, in parallel, derives its cell, pre-culls it against the
-//      horizon at the start of the chunk, fetches the column-table entry and
-//      scans the column's runs; a __ballot_sync gives the cells that may draw;
+//      horizon at the start of the chunk, fetches the column-table entry,
+//      scans the column's runs and records in shared memory the runs the
+//      walk could still draw, with their span constants; a __ballot_sync
+//      gives the cells that may draw;
 //   3. the group walks those cells in order (values broadcast with
-//      __shfl_sync) and applies the exact sequential horizon logic; span
-//      pixels are interpolated and written by all G lanes at once.
+//      __shfl_sync) and applies the exact sequential horizon logic to the
+//      recorded runs; span pixels are interpolated and written by all G
+//      lanes at once, or, for short spans, claimed in the bitmask and
+//      coloured later G samples at a time.
 // The pre-cull is conservative: the horizon only closes (ymin grows, ymax
 // shrinks), so a cell or run culled at the chunk start would be culled at
 // its turn too.  The result is the sequential algorithm's, bit for bit.
