@@ -51,16 +51,27 @@ def oracle_counters(cnt) -> dict:
     return {n: int(cnt[n].sum()) for n in cnt.dtype.names}
 
 
+def float_bits(a: np.ndarray) -> np.ndarray:
+    """The bits of a float32 array with every NaN as 0x7fc00000.  A NaN's
+    bit pattern is the platform's (x86 hosts give 0xffc00000, Arm hosts
+    0x7fc00000, the GPU 0x7fffffff); a degenerate span (zero screen height,
+    a camera inside the ground) makes NaN depths on every platform, so NaN
+    must meet NaN at the same sample, and every other value bit for bit."""
+    bits = a.view(np.uint32).copy()
+    bits[np.isnan(a)] = 0x7FC00000
+    return bits
+
+
 def assert_rays_equal(gpu, orc, label=""):
-    """Packed words and hits bit-exact; depth bit-exact too (the stated bar
-    is 1e-5 relative, the implementation meets it with zero error)."""
+    """Packed words and hits bit-exact; depth bit-exact too, NaN matching NaN
+    (the stated bar is 1e-5 relative, the implementation meets it with zero
+    error)."""
     gw, gd, gh, _ = gpu
     ow, od, oh, _ = orc
     assert gw.shape == ow.shape, label
     bad = int((gw != ow).sum())
     assert bad == 0, f"{label}: {bad} of {gw.size} ray-buffer words differ"
-    gbits, obits = gd.view(np.uint32), od.view(np.uint32)
-    dbad = int((gbits != obits).sum())
-    assert dbad == 0, f"{label}: {dbad} depths differ (max rel {np.nanmax(np.abs(gd - od) / np.abs(od)):.3g})"
+    dbad = int((float_bits(gd) != float_bits(od)).sum())
+    assert dbad == 0, f"{label}: {dbad} depths differ"
     if gh is not None and oh is not None:
         assert np.array_equal(gh, oh), f"{label}: {int((gh != oh).sum())} hit records differ"

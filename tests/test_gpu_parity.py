@@ -8,7 +8,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from gpu_util import Frame, assert_rays_equal, counters_dict, oracle_counters
+from gpu_util import Frame, assert_rays_equal, counters_dict, float_bits, oracle_counters
 
 pytestmark = pytest.mark.gpu
 
@@ -94,7 +94,7 @@ def test_config1_frame(rle, po, scene512, torch_cuda):
     col, dep, hit = fr.resolve_host()
     ocol, odep, ohit, _ = po.resolve(om, 640, 480, orc[0], orc[1], orc[2])
     assert np.array_equal(col, ocol), f"{int((col != ocol).sum())} pixels differ"
-    assert np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
+    assert np.array_equal(float_bits(dep), float_bits(odep))
     assert np.array_equal(hit, ohit)
     assert (col != 0xFFFFCCB2).mean() > 0.3  # terrain is visible
 
@@ -130,7 +130,7 @@ def test_cave_scene_poses(rle, po, caves256, torch_cuda, pose):
     assert_rays_equal(fast, orc, f"{pose} (no counters)")
     col, dep, hit = fr.resolve_host()
     ocol, odep, ohit, _ = po.resolve(om, W, H, orc[0], orc[1], orc[2])
-    assert np.array_equal(col, ocol) and np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
+    assert np.array_equal(col, ocol) and np.array_equal(float_bits(dep), float_bits(odep))
     assert np.array_equal(hit, ohit)
 
 
@@ -175,7 +175,7 @@ def test_maximum_samples(rle, po, caves256, torch_cuda, pose):
     assert_rays_equal(fast, orc, f"S=16384 {pose} (no counters)")
     col, dep, hit = fr.resolve_host()
     ocol, odep, ohit, _ = po.resolve(om, 400, 300, orc[0], orc[1], orc[2])
-    assert np.array_equal(col, ocol) and np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
+    assert np.array_equal(col, ocol) and np.array_equal(float_bits(dep), float_bits(odep))
     assert np.array_equal(hit, ohit)
     with pytest.raises(rle.RLEError):
         rle.raymap_build(cam, rle.view_params(400, 300, samples=16385))

@@ -12,7 +12,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from gpu_util import Frame, assert_rays_equal
+from gpu_util import Frame, assert_rays_equal, float_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +45,7 @@ def test_config2_full_frames(rle, po, torch_cuda):
         col, dep, _ = fr.resolve_host()
         ocol, odep, _, _ = po.resolve(om, 1920, 1080, orc[0], orc[1], orc[2])
         assert np.array_equal(col, ocol), f"pose {k}: {int((col != ocol).sum())} pixels differ"
-        assert np.array_equal(dep.view(np.uint32), odep.view(np.uint32))
+        assert np.array_equal(float_bits(dep), float_bits(odep))
     scene.free()
 
 
