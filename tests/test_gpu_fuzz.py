@@ -77,3 +77,47 @@ def test_random_scene_view_camera(rle, po, torch_cuda, case):
     assert np.array_equal(float_bits(dep), float_bits(odep)), label
     assert np.array_equal(hit, ohit), label
     scene.free()
+
+
+@pytest.mark.parametrize("case", range(12))
+def test_random_batches(rle, po, torch_cuda, case):
+    """Batches of 2-6 random views and cameras of one random scene, under a
+    random launch shape (claim tile, lanes per ray, staging, graph or not,
+    one launch pair per frame or not), equal the frames rendered one by one:
+    colour, depth (NaN meeting NaN) and hit records."""
+    torch = torch_cuda
+    rng = np.random.default_rng(7000 + case)
+    scene, oscene, n, sy = _scene(rle, po, rng)
+    frames = []
+    for _ in range(int(rng.integers(2, 7))):
+        view = _view(rle, rng)
+        frames.append((_camera(rle, rng, oscene, n, sy), view))
+    outs = []
+    for cam, view in frames:
+        px = view.width * view.height
+        outs.append((torch.full((px,), 7, dtype=torch.int32, device="cuda"),
+                     torch.full((px,), 7.0, dtype=torch.float32, device="cuda"),
+                     torch.zeros(px * 8, dtype=torch.uint8, device="cuda")))
+    reqs = [rle.frame_request(c, v, *o) for (c, v), o in zip(frames, outs)]
+    max_s = max(rle.raymap_build(c, v).samples for c, v in frames)
+    b = rle.Batch(len(frames), rle.batch_words_needed(reqs), max_s, with_hits=True)
+    shape = (int(rng.choice([1, 2, 4, 16])), int(rng.choice([8, 16, 32])), int(rng.integers(1, 4)),
+             int(rng.choice([32, 64, 128])), int(rng.integers(0, 2)), int(rng.integers(0, 2)))
+    b.set_tuning(*shape)
+    b.render(scene, reqs)
+    torch.cuda.synchronize()
+    for k, (cam, view) in enumerate(frames):
+        ws_bytes = rle.frame_workspace_bytes(view)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+        px = view.width * view.height
+        c = torch.empty(px, dtype=torch.int32, device="cuda")
+        d = torch.empty(px, dtype=torch.float32, device="cuda")
+        h = torch.empty(px * 8, dtype=torch.uint8, device="cuda")
+        rle.render_frame(scene, cam, view, ws, ws_bytes, c, d, h)
+        torch.cuda.synchronize()
+        label = f"case {case} frame {k} shape {shape}"
+        assert torch.equal(outs[k][0], c), label
+        assert np.array_equal(float_bits(outs[k][1].cpu().numpy()), float_bits(d.cpu().numpy())), label
+        assert torch.equal(outs[k][2], h), label
+    b.free()
+    scene.free()
