@@ -165,3 +165,43 @@ def test_raymap_and_raycast_match_reference(po):
         total += out.size
         diff += int((out != ref).sum())
     assert diff == 0, f"{diff} of {total} samples differ"
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [31, 32, 33])
+def test_raycast_matches_reference_random(po, seed):
+    """Wider random sweep against the reference's host build: grid 32-128,
+    4 mip levels, eyes above the scene's top, inside it and under the
+    ground, pitch up to +-89 degrees, ray-buffer rows of 64-256 samples
+    (not only multiples of 32), random ray counts, borders, switch and far
+    distances."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.choice([32, 64, 128]))
+    vol = _random_volume(n, seed)
+    bits = [po.pack_bits(vol)]
+    dims = [(n, n, n)]
+    for _ in range(3):
+        bits.append(po.mipmap(bits[-1], *dims[-1]))
+        dims.append(tuple(d // 2 for d in dims[-1]))
+    levels = [(*dims[m], po.encode_mip(bits[m], *dims[m], m)[1]) for m in range(4)]
+    scene = po.OracleScene(levels)
+    total = diff = 0
+    for k in range(12):
+        S = int(rng.choice([64, 100, 160, 256]))
+        maxres = int(rng.integers(16, S + 1))
+        border = float(rng.uniform(0.0, 0.3))
+        mipd = int(rng.integers(16, 129))
+        zfar = int(rng.integers(200, 3001))
+        pos = (float(rng.uniform(-0.5 * n, 1.5 * n)), float(rng.uniform(-2.0 * n, 0.5 * n)),
+               float(rng.uniform(-0.5 * n, 1.5 * n)))
+        rot = (float(rng.choice([-1, 1]) * rng.uniform(0.02, 1.55)), float(rng.uniform(0, 6.3)), 0.0)
+        rb = po.ref_raymap(pos, rot, border, maxres)
+        rm = po.raymap_build(pos, rot, border, maxres, 1.0, S, mipd, zfar)
+        assert list(rm.res) == list(po.ref_raymap_fields(rb)["res"]), f"pose {k}"
+        nr = po.rays_to_render(rm)
+        ref = po.ref_render_rays(rb, scene, S, nr, mipd, zfar)
+        out, _, _, _ = po.render_rays(rm, scene)
+        total += out.size
+        diff += int((out != ref).sum())
+    assert total > 0
+    assert diff == 0, f"{diff} of {total} samples differ"
