@@ -1,12 +1,14 @@
 """Render frames of a seeded scene from the command line.
 
     python rle-based-voxel-raycasting_gb300/render_frames.py [--size 2048] [--height 256] [--seed 2]
-        [--width 1920] [--screen-height 1080] [--frames 6] [--fov 90] [--png-dir DIR] [--batch N]
+        [--width 1920] [--screen-height 1080] [--frames 6] [--fov 90] [--png-dir DIR] [--batch N] [--json]
 
 Builds the scene on the GPU (rle_scenegen_device), walks a seeded camera
 path (poses 10-80 voxels above the ground, yaw uniform, pitch up to 30
 degrees) and renders each frame with rle_render_frame, printing the time per
-frame; with --png-dir it also writes every frame as a PNG.  This is the
+frame; with --png-dir it also writes every frame as a PNG; with --json it
+prints one JSON object per line instead (frame or batch index, frames,
+milliseconds, screen pixels, Mrays/s, column rays, samples per ray).  This is the
 headless counterpart of the reference's interactive viewer
 (src/main.cpp:446-669): the frame ends in device buffers, not in a window.
 """
@@ -14,6 +16,7 @@ from __future__ import annotations
 
 import argparse
 import importlib.util
+import json
 import struct
 import sys
 import time
@@ -48,6 +51,12 @@ def write_png(path: Path, rgb: np.ndarray) -> None:
                      chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
 
 
+def _metrics(index: int, frames: int, ms: float, pixels: int, rays: int, samples: int) -> dict:
+    return {"index": index, "frames": frames, "ms": round(ms, 4), "pixels": pixels,
+            "mrays_per_s": round(pixels / ms / 1e3, 1) if ms > 0 else None, "column_rays": rays,
+            "samples_per_ray": samples}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--size", type=int, default=2048, help="scene columns along x and z (power of two)")
@@ -66,6 +75,7 @@ def main(argv=None) -> int:
                     help="render the path in batches of this many frames (rle_batch, autotuned) instead")
     ap.add_argument("--batch-lanes", type=int, default=0,
                     help="with --batch: skip the autotuner, one-ray claims with this many lanes per ray")
+    ap.add_argument("--json", action="store_true", help="one JSON object per frame (or batch) on stdout")
     args = ap.parse_args(argv)
 
     import torch
@@ -106,7 +116,12 @@ def main(argv=None) -> int:
         rle.render_frame(scene, cam, view, ws, ws_bytes, colour, depth)
         e1.record()
         torch.cuda.synchronize()
-        print(f"frame {i}: {e0.elapsed_time(e1):.3f} ms", flush=True)
+        ms = e0.elapsed_time(e1)
+        if args.json:
+            rm = rle.raymap_build(cam, view)
+            print(json.dumps(_metrics(i, 1, ms, W * H, rm.rays, rm.samples)), flush=True)
+        else:
+            print(f"frame {i}: {ms:.3f} ms", flush=True)
         if out_dir:
             rgba = colour.cpu().numpy().view(np.uint8).reshape(H, W, 4)
             write_png(out_dir / f"frame_{i:04d}.png", np.ascontiguousarray(rgba[:, :, :3]))
@@ -133,15 +148,21 @@ def _batched(rle, torch, scene, info, table, words, rng, view, args) -> int:
         b.set_tuning(1, args.batch_lanes, 1, 128)
     else:
         best, ms = b.autotune(scene, groups[0], repeats=1)
-        print(f"autotuned: tile {best.tile_rays} lanes {best.lanes_per_ray} staging {best.staging} "
-              f"per_frame {best.per_frame} ({ms:.3f} ms)", flush=True)
+        msg = (f"autotuned: tile {best.tile_rays} lanes {best.lanes_per_ray} staging {best.staging} "
+               f"per_frame {best.per_frame} ({ms:.3f} ms)")
+        print(msg, file=sys.stderr if args.json else sys.stdout, flush=True)
     for i, g in enumerate(groups):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         b.render(scene, g)
         e1.record()
         torch.cuda.synchronize()
-        print(f"batch {i}: {len(g)} frames, {e0.elapsed_time(e1):.3f} ms", flush=True)
+        ms = e0.elapsed_time(e1)
+        if args.json:
+            rays = sum(rle.raymap_build(r.cam, r.view).rays for r in g)
+            print(json.dumps(_metrics(i, len(g), ms, W * H * len(g), rays, view.samples)), flush=True)
+        else:
+            print(f"batch {i}: {len(g)} frames, {ms:.3f} ms", flush=True)
     b.free()
     scene.free()
     return 0
