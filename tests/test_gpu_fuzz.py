@@ -10,6 +10,8 @@ meet NaN at the same sample; their bit patterns are the platform's).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 import pytest
 
@@ -17,7 +19,8 @@ from gpu_util import Frame, assert_rays_equal, counters_dict, float_bits, oracle
 
 pytestmark = pytest.mark.gpu
 
-CASES = 64
+# RLE_FUZZ_CASES widens the sweep (the default keeps the suite quick)
+CASES = int(os.environ.get("RLE_FUZZ_CASES", "64"))
 
 
 def _scene(rle, po, rng):
@@ -79,7 +82,7 @@ def test_random_scene_view_camera(rle, po, torch_cuda, case):
     scene.free()
 
 
-@pytest.mark.parametrize("case", range(12))
+@pytest.mark.parametrize("case", range(max(12, CASES // 5)))
 def test_random_batches(rle, po, torch_cuda, case):
     """Batches of 2-6 random views and cameras of one random scene, under a
     random launch shape (claim tile, lanes per ray, staging, graph or not,
