@@ -150,3 +150,58 @@ def test_device_encoder_matches_generator_volume(rle, po, torch_cuda):
         assert np.array_equal(got[m][3], want[m][3]) and np.array_equal(got[m][4], want[m][4]), f"level {m}"
     scene.free()
     ref.free()
+
+
+def _random_volume_kind(rng, sx, sy, sz, kind):
+    """Volumes [z, y, x] of several kinds: noise of a random density, thin
+    horizontal layers (many runs per column), a single voxel, empty, full,
+    and the smooth blobs."""
+    if kind == "noise":
+        return rng.random((sz, sy, sx)) < rng.uniform(0.05, 0.95)
+    if kind == "layers":
+        rows = rng.random(sy) < 0.5
+        return np.broadcast_to(rows[None, :, None], (sz, sy, sx)).copy()
+    if kind == "voxel":
+        v = np.zeros((sz, sy, sx), bool)
+        v[rng.integers(0, sz), rng.integers(0, sy), rng.integers(0, sx)] = True
+        return v
+    if kind == "empty":
+        return np.zeros((sz, sy, sx), bool)
+    if kind == "full":
+        return np.ones((sz, sy, sx), bool)
+    return _blob_volume(sx, sy, sz, int(rng.integers(0, 1 << 20)))
+
+
+@pytest.mark.parametrize("case", range(12))
+def test_device_encoder_random_volumes(rle, po, torch_cuda, case):
+    """Random grids (x, z powers of two 8-128, heights 1-1024 -- runs longer
+    than a 6-bit solid count or a 10-bit skip split as the reference splits
+    them --, up to 4 levels) and volume kinds, with or without colours:
+    every level's slab words and column table equal the oracle's."""
+    torch = torch_cuda
+    rng = np.random.default_rng(500 + case)
+    sx, sz = (int(rng.choice([8, 16, 32, 64, 128])) for _ in range(2))
+    sy = int(rng.choice([1, 7, 64, 100, 257, 1024]))
+    kind = ["noise", "layers", "voxel", "empty", "full", "blobs"][case % 6]
+    if kind in ("voxel", "full") and case >= 6:
+        sy = 1024  # the longest skip (1023) and 16 solid runs per column
+    nummaps = int(rng.integers(1, 5))
+    # levels keep x and z at 8 or more (the Tree layout packs 8 voxels of x
+    # per byte) and at least one voxel of height
+    while nummaps > 1 and (min(sx, sz) >> (nummaps - 1) < 8 or sy >> (nummaps - 1) < 1):
+        nummaps -= 1
+    vol = _random_volume_kind(rng, sx, sy, sz, kind)
+    bits = po.pack_bits(vol)
+    colours = rng.integers(0, 65536, sx * sy * sz, dtype=np.uint16) if case % 2 else None
+    want = _oracle_levels(po, bits, colours, sx, sy, sz, nummaps)
+    d_bits = torch.from_numpy(bits).cuda()
+    d_col = torch.from_numpy(colours.view(np.int16)).cuda() if colours is not None else None
+    scene = rle.Scene.encode_on_device(d_bits, d_col, sx, sy, sz, nummaps)
+    _, got = _levels(rle, scene)
+    label = f"case {case}: {sx}x{sy}x{sz} {kind} levels {nummaps} colours {colours is not None}"
+    assert len(got) == len(want), label
+    for m, (a, b) in enumerate(zip(want, got)):
+        assert a[:3] == b[:3], f"{label}: level {m} size"
+        assert np.array_equal(a[4], b[4]), f"{label}: level {m} slab words"
+        assert np.array_equal(a[3], b[3]), f"{label}: level {m} table"
+    scene.free()
