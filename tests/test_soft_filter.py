@@ -87,3 +87,31 @@ def test_kernel_equals_oracle_on_rendered_frames(rle, po, torch_cuda, res):
         # the filter changes something on a real frame (edges and depth steps)
         assert np.count_nonzero((got & 0xFFFFFF) != (c & 0xFFFFFF)) > 0
     scene.free()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("res", [(1, 1), (7, 3), (33, 9), (100, 75), (2048, 17), (17, 2048), (257, 129)])
+def test_kernel_equals_oracle_on_random_frames(rle, po, torch_cuda, res):
+    """Frame sizes that are not multiples of the kernel's 32 x 8 tile (and
+    smaller than its 12-pixel apron), the largest width and height, random
+    colours and depths mixing finite values, sky (+inf), no data (0), NaN and
+    negative depths."""
+    torch = torch_cuda
+    W, H = res
+    rng = np.random.default_rng(W * 4099 + H)
+    c = rng.integers(0, 1 << 32, W * H, dtype=np.uint64).astype(np.uint32)
+    d = rng.uniform(1.0, 5000.0, W * H).astype(np.float32)
+    kind = rng.integers(0, 10, W * H)
+    d[kind == 0] = np.inf
+    d[kind == 1] = 0.0
+    d[kind == 2] = np.nan
+    d[kind == 3] = -d[kind == 3]
+    d[kind == 4] = rng.uniform(0.0, 2.0, int((kind == 4).sum())).astype(np.float32)
+    colour = torch.from_numpy(c.view(np.int32)).cuda()
+    depth = torch.from_numpy(d).cuda()
+    out = torch.full((W * H,), 7, dtype=torch.int32, device="cuda")
+    rle.soft_filter(colour, depth, W, H, out)
+    torch.cuda.synchronize()
+    want = po.soft_filter(c, d, W, H)
+    got = out.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, want), f"{res}: {np.count_nonzero(got != want)} pixels differ"
