@@ -37,6 +37,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 PKG_DIR = ROOT / "rle-based-voxel-raycasting_gb300"
 METRIC = "primary Mrays/s @1080p (plain per-frame launch, 2048^2 cave scene)"
+WORKLOAD = ("config 2: 2048x2048x256 cave scene seed 2, 1920x1080 frames, 90 deg FOV, "
+            "poses 10-80 above ground, yaw U[0,360), pitch U[-30,30]")
 W, H = 1920, 1080
 SCENE = dict(n=2048, sy=256, seed=2, caves=True)
 
@@ -335,8 +337,7 @@ def run_ours(args):
         "dtype": "f32",
         "data": "synthetic (seeded scene and camera path)",
         "config": {
-            "workload": "config 2: 2048x2048x256 cave scene seed 2, 1920x1080 frames, 90 deg FOV, "
-                        "poses 10-80 above ground, yaw U[0,360), pitch U[-30,30]",
+            "workload": WORKLOAD,
             "scene_device_bytes": int(info.device_bytes),
             "runs_per_column": round(info.run_headers / (SCENE["n"] ** 2), 2),
             "column_rays_per_frame": round(sum(rays) / len(rays), 1),
@@ -650,14 +651,18 @@ def run_reference(args):
     view = frame_view(rle, W, H)
     threads = os.cpu_count() or 1
 
+    rays = []
+
     def frame(c):
         rm = rle.raymap_build(c, view)
+        rays.append(rm.rays)
         om = po.raymap_from_product(rm)
         out, dep, _, _ = po.render_rays(om, oscene, nthreads=threads)
         po.resolve(om, W, H, out, dep)
 
     for c in cams[:args.warmup]:
         frame(c)
+    rays.clear()  # the timed frames' rays only
     t0 = time.perf_counter()
     for c in cams[args.warmup:]:
         frame(c)
@@ -667,8 +672,9 @@ def run_reference(args):
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and camera path)",
-        "config": {"workload": "config 2: 2048x2048x256 cave scene seed 2, 1920x1080 frames, 90 deg FOV, "
-                               "poses 10-80 above ground, yaw U[0,360), pitch U[-30,30]"},
+        "config": {"workload": WORKLOAD, "samples_per_ray": view.samples,
+                   "column_rays_per_frame": round(sum(rays) / len(rays), 1),
+                   "parallelism": f"host: OpenMP over column rays, {threads} threads"},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} frame(s): ray map + Render::render_line port + resolve, "
