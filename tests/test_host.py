@@ -123,6 +123,24 @@ def test_invalid_arguments_return_status(rle):
     assert lib.rle_encode_device(fake, None, 48, 64, 64, 4, 0, C.byref(h)) == -1  # sx not a power of two
     assert lib.rle_encode_device(fake, None, 64, 2048, 64, 4, 0, C.byref(h)) == -1  # sy > 1024
     assert lib.rle_encode_device(fake, None, 8, 64, 64, 5, 0, C.byref(h)) == -1  # 8 >> 4 == 0
+    # batch and server limits are checked before any device work
+    assert lib.rle_batch_create(0, 0, 1 << 20, 1024, 0, C.byref(h)) == -1        # no frames
+    assert lib.rle_batch_create(0, 4, 16, 1024, 0, C.byref(h)) == -1             # ray buffer < 32 words
+    assert lib.rle_batch_create(0, 4, 1 << 20, 16385, 0, C.byref(h)) == -1       # samples beyond 16384
+    assert lib.rle_batch_create(0, 65537, 1 << 20, 1024, 0, C.byref(h)) == -1    # too many frames
+    cfg = rle.ServerConfig(0, 1 << 30, 8, 0, 1 << 20, 1024, 0)                   # no in-flight slot
+    assert lib.rle_server_create(C.byref(cfg), C.byref(h)) == -1
+    cfg = rle.ServerConfig(0, 1 << 30, 8, 17, 1 << 20, 1024, 0)                  # more than 16 slots
+    assert lib.rle_server_create(C.byref(cfg), C.byref(h)) == -1
+    cfg = rle.ServerConfig(0, 1 << 30, 8, 2, 1 << 20, 4, 0)                      # samples below 8
+    assert lib.rle_server_create(C.byref(cfg), C.byref(h)) == -1
+    assert lib.rle_server_create(None, C.byref(h)) == -1
+    # the process-wide launch shape accepts only the built shapes
+    with pytest.raises(rle.RLEError):
+        rle.tuning_set(lanes_per_ray=12)
+    with pytest.raises(rle.RLEError):
+        rle.tuning_set(threads_per_block=48)
+    assert rle.tuning_get() == (0, 0, 0)
 
 
 def test_malformed_rle4_rejected_before_upload(rle, po):
