@@ -282,6 +282,24 @@ rle_status rle_render_rays(const rle_scene* scene, const rle_raymap* rm, uint32_
                            float* d_raydepth, rle_hit* d_rayhit, rle_counters* d_counters,
                            void* stream);
 
+/* When each column ray of one launch ran: the timing counterpart of the
+ * reference's per-ray DETAIL_BENCH records (src/Cuda_Render.h:14-22, summed
+ * at src/Cuda_Main.cu:244-267), for profiling.  A frame cannot end before
+ * its slowest ray: end_clock - start_clock of that ray, at the SM clock,
+ * bounds the launch from below. */
+typedef struct rle_ray_time {
+    uint64_t start_ns, end_ns;        /* %globaltimer (ns, the same clock on every SM) */
+    uint64_t start_clock, end_clock;  /* clock64() of the SM that cast the ray */
+    uint32_t sm;                      /* that SM (%smid) */
+    uint32_t reserved;
+} rle_ray_time;
+
+/* rle_render_rays without hit records or counters (the production kernel the
+ * benchmark times) that also writes d_times[r] for every cast ray
+ * r < rm->rays.  The two timestamps per ray are the only extra work. */
+rle_status rle_render_rays_timed(const rle_scene* scene, const rle_raymap* rm, uint32_t* d_raybuf,
+                                 float* d_raydepth, rle_ray_time* d_times, void* stream);
+
 /* The colorize shader's resolve as a kernel: per screen pixel (row 0 at the
  * top), the ray-buffer sample its fan geometry selects.
  *   d_colour RGBA8 (R in the low byte): RGB565 expanded, sky 0xFFFFCCB2, none 0
@@ -344,7 +362,9 @@ rle_status rle_batch_get_tuning(const rle_batch* b, rle_batch_tuning* t);
 /* Ray-buffer words a set of frames needs (0 if a camera or view is invalid). */
 size_t rle_batch_words_needed(const rle_frame_request* frames, int n);
 /* Renders n frames; outputs as rle_render_frame.  Asynchronous on `stream`;
- * one batch object renders one batch at a time (calls are serialised). */
+ * one batch object renders one batch at a time: calls are serialised on the
+ * host, and a call's device work waits for the previous call's (which shares
+ * the batch's ray buffer and parameter block), whatever streams they use. */
 rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                             void* stream);
 /* Times every tile_rays x lanes_per_ray x staging combination
@@ -389,6 +409,8 @@ typedef struct rle_completion {
     uint64_t ticket;
     rle_status status;
     double submit_s, launch_s, done_s;  /* host monotonic clock, seconds */
+    double gpu_ms;  /* device time of the launch that carried the request (CUDA events
+                       before and after it on the slot's stream); 0 if it never ran */
 } rle_completion;
 
 typedef struct rle_server_stats {
@@ -434,12 +456,20 @@ rle_status rle_server_destroy(rle_server* s);
  * the device), or a plug-in whose host application owns the GPU memory
  * budget.  Same result as rle_render_frame without hit records.
  * The ray buffer lives in a fixed array built into the library:
- * rle_render_frame_noalloc_limit() bytes (64 MiB) on every device that loads
- * the library, held until the process exits.  A frame needs
- * 8 x rays x samples bytes of it (e.g. 1080p with up to ~4300 column rays);
- * larger frames return RLE_ERR_CAPACITY.
- * The first call on a device looks up the array's device address (with that
- * device current); make that first call before any stream capture.
+ * rle_render_frame_noalloc_limit() bytes (64 MiB) per device, held until the
+ * process exits.  A frame needs 8 x rays x samples bytes of it (e.g. 1080p
+ * with up to ~4300 column rays); larger frames return RLE_ERR_CAPACITY.
+ * When the array is reserved: CUDA loads a library's device code lazily by
+ * default (CUDA 12.2 and later), so the array is reserved on a device by the
+ * first call on that device, which also looks up its device address (with
+ * that device current).  That first call can therefore allocate, wait for
+ * the device or fail with RLE_ERR_CUDA if the device has no room: make it at
+ * start-up, before the frame loop and before any stream capture.  Later calls
+ * allocate nothing.  With CUDA_MODULE_LOADING=EAGER in the environment the
+ * array is reserved when the library loads instead.
+ * The looked-up address is kept for the life of the process: after a
+ * cudaDeviceReset of that device it is stale, so do not call this entry
+ * point on a device that was reset.
  * All calls share the one array: calls whose work can overlap on the GPU
  * (different streams, or host threads without ordering) race -- issue them on
  * one stream.  Nothing in the array needs clearing: every word a frame reads

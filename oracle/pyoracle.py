@@ -18,7 +18,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref.so"
-REF_SRC = Path("/root/reference/RLE-Raycaster")
+# The reference checkout is located by the recipe in ref/Makefile: the
+# RLE_REF_SRC environment variable, else the recipe's default location.
+REF_RECIPE = HERE / "ref"
 
 
 def _foreign(path: Path) -> bool:
@@ -46,12 +48,24 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
+def ref_checkout_present() -> bool:
+    """Whether the recipe finds the reference checkout (RLE_REF_SRC or its
+    default location)."""
+    try:
+        r = subprocess.run(["make", "-s", "-C", str(REF_RECIPE), "check-ref"], stdout=subprocess.DEVNULL,
+                           stderr=subprocess.DEVNULL)
+    except OSError:  # no make on this host
+        return False
+    return r.returncode == 0
+
+
 def build_ref() -> Optional[Path]:
-    """Compile the reference's host sources (only where the checkout exists)."""
-    if not REF_SRC.exists():
-        return REF_LIB if REF_LIB.exists() else None
-    subprocess.run(["make", "-s", "-C", str(HERE / "ref"), f"REF={REF_SRC}"], check=True,
-                   stdout=subprocess.DEVNULL)
+    """Compile the reference's host sources where the checkout exists (see
+    ref/Makefile); elsewhere return the library built earlier, or None (the
+    tests that need it then skip, saying so)."""
+    if not ref_checkout_present():
+        return REF_LIB if REF_LIB.exists() and not _foreign(REF_LIB) else None
+    subprocess.run(["make", "-s", "-C", str(REF_RECIPE)], check=True, stdout=subprocess.DEVNULL)
     return REF_LIB
 
 
@@ -110,7 +124,8 @@ def ref() -> C.CDLL:
     global _ref
     if _ref is None:
         if not REF_LIB.exists():
-            raise FileNotFoundError("oracle/_ref/libref.so not built (needs the reference checkout)")
+            raise FileNotFoundError("oracle/_ref/libref.so not built: it needs the reference checkout "
+                                    "(set RLE_REF_SRC to its RLE-Raycaster folder and run build_ref())")
         lib = C.CDLL(str(REF_LIB))
         lib.ref_get_ray_map.argtypes = [C.c_float] * 7 + [C.c_int, C.c_void_p]
         lib.ref_render_rays.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -113,7 +113,7 @@ class Request(C.Structure):
 
 class Completion(C.Structure):
     _fields_ = [("ticket", C.c_uint64), ("status", C.c_int), ("submit_s", C.c_double), ("launch_s", C.c_double),
-                ("done_s", C.c_double)]
+                ("done_s", C.c_double), ("gpu_ms", C.c_double)]
 
 
 class ServerStats(C.Structure):
@@ -168,6 +168,7 @@ def _load() -> C.CDLL:
         "rle_tuning_set": (C.c_int, [C.POINTER(Tuning)]),
         "rle_tuning_get": (C.c_int, [C.POINTER(Tuning)]),
         "rle_render_rays": (C.c_int, [vp, C.POINTER(RayMap), vp, vp, vp, vp, vp]),
+        "rle_render_rays_timed": (C.c_int, [vp, C.POINTER(RayMap), vp, vp, vp, vp]),
         "rle_resolve": (C.c_int, [C.POINTER(RayMap), vp, vp, vp, vp, vp, vp, vp]),
         "rle_frame_workspace_bytes": (C.c_size_t, [C.POINTER(ViewParams)]),
         "rle_render_frame": (C.c_int, [vp, C.POINTER(Camera), C.POINTER(ViewParams), vp, C.c_size_t, vp, vp, vp, vp]),
@@ -389,6 +390,19 @@ def tuning_get() -> tuple[int, int, int]:
 def render_rays(scene: Scene, rm: RayMap, raybuf, raydepth, rayhit=None, counters=None, stream: int = 0) -> None:
     _check(_lib.rle_render_rays(scene.handle, C.byref(rm), ptr(raybuf), ptr(raydepth), ptr(rayhit),
                                 ptr(counters), stream or None), "rle_render_rays")
+
+
+# rle_ray_time: per-ray start/end of one raycast launch (rle_render_rays_timed)
+RAY_TIME_DTYPE = np.dtype([("start_ns", "<u8"), ("end_ns", "<u8"), ("start_clock", "<u8"), ("end_clock", "<u8"),
+                           ("sm", "<u4"), ("reserved", "<u4")])
+
+
+def render_rays_timed(scene: Scene, rm: RayMap, raybuf, raydepth, times, stream: int = 0) -> None:
+    """rle_render_rays (production kernel, no hits or counters) that also
+    writes an rle_ray_time record per cast ray into `times` (a device buffer
+    of at least rm.rays * 40 bytes)."""
+    _check(_lib.rle_render_rays_timed(scene.handle, C.byref(rm), ptr(raybuf), ptr(raydepth), ptr(times),
+                                      stream or None), "rle_render_rays_timed")
 
 
 def resolve(rm: RayMap, raybuf, raydepth, colour, depth, rayhit=None, hit=None, stream: int = 0) -> None:

@@ -216,6 +216,13 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
     }
     rle_status st = stage_frames(b, scene, scenes, frames, n, b->h_params[par]);
     if (st != RLE_OK) return st;
+    // The previous call's launches use the same device parameter block and
+    // ray buffer; on another stream they may still be running, so this
+    // call's device work waits for them (a no-op on the same stream).
+    if (b->staged_used[par ^ 1]) {
+        const cudaError_t e = cudaStreamWaitEvent(stream, b->staged[par ^ 1], 0);
+        if (e != cudaSuccess) return cuda_fail(e, "rle_batch_render: ordering after the previous batch");
+    }
     if (!b->raycast_blocks) {
         st = prepare_grid(b);
         if (st != RLE_OK) return st;

@@ -186,6 +186,29 @@ extern "C" rle_status rle_render_rays(const rle_scene* scene, const rle_raymap* 
     return rle::launch_raycast(p, stream);
 }
 
+extern "C" rle_status rle_render_rays_timed(const rle_scene* scene, const rle_raymap* rm, uint32_t* d_raybuf,
+                                            float* d_raydepth, rle_ray_time* d_times, void* stream) {
+    if (!scene || !rm || !d_raybuf || !d_raydepth || !d_times) {
+        rle::set_error("rle_render_rays_timed: scene, ray map, ray/depth buffers and the time records are required");
+        return RLE_ERR_INVALID_ARG;
+    }
+    rle::RayParams p;
+    rle_status st = rle::fill_ray_params(scene, rm, &p);
+    if (st != RLE_OK) return st;
+    p.raybuf = d_raybuf;
+    p.raydepth = d_raydepth;
+    p.ray_time = d_times;
+    p.lanes_per_ray = g_lanes_per_ray;
+    p.cells_per_lane = g_cells_per_lane;
+    p.threads_per_block = g_threads_per_block;
+    rle::DeviceGuard g(scene->device);
+    if (!g.ok) {
+        rle::set_error("rle_render_rays_timed: cannot select device %d", scene->device);
+        return RLE_ERR_CUDA;
+    }
+    return rle::launch_raycast(p, stream);
+}
+
 extern "C" rle_status rle_resolve(const rle_raymap* rm, const uint32_t* d_raybuf, const float* d_raydepth,
                                   const rle_hit* d_rayhit, uint32_t* d_colour, float* d_depth, rle_hit* d_hit,
                                   void* stream) {

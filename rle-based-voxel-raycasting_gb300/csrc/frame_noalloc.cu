@@ -6,8 +6,11 @@
 // call can synchronise the device and stall the frame), and a plug-in hosted
 // by an application that owns the GPU memory budget may not allocate at all.
 // For them this entry point keeps the ray buffer in a fixed array compiled
-// into the library, reserved on each device that loads the library until the
-// process exits.
+// into the library.  Device code is loaded lazily (the CUDA default since
+// 12.2), so the array is reserved on a device by the first call there, which
+// also looks up its address; it stays reserved until the process exits, and
+// later calls allocate nothing.  The cached address does not survive a
+// cudaDeviceReset of the device.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -95,6 +95,18 @@ __device__ __forceinline__ F3 to3d(const RayParams& P, F3 v) {
               P.to3d[0][2] * v.x + P.to3d[1][2] * v.y + P.to3d[2][2] * v.z + P.to3d[3][2]);
 }
 
+// Device-wide nanosecond clock and the SM a thread runs on (profiling).
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t sm_id() {
+    uint32_t s;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(s));
+    return s;
+}
+
 // First lane of the group a lane mask describes.
 __device__ __forceinline__ int lane_base(unsigned gmask) { return __ffs(gmask) - 1; }
 
@@ -1091,7 +1103,21 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
         kDefer ? recs + static_cast<size_t>(blockDim.x) * (3 * kRecs) + static_cast<size_t>(L.slot) * (kQueueVecs * G)
                : nullptr;
     Counts cnt;
+    // per-ray timing (rle_render_rays_timed): the first lane of the group
+    // stamps the ray's start and end; nothing else changes
+    if (P.ray_time && L.k == 0 && x < P.rays) {
+        rle_ray_time* t = P.ray_time + x;
+        t->start_ns = global_ns();
+        t->start_clock = static_cast<uint64_t>(clock64());
+    }
     cast_ray<G, kCount, kHits, kDefer>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, cnt);
+    if (P.ray_time && L.k == 0 && x < P.rays) {
+        rle_ray_time* t = P.ray_time + x;
+        t->end_clock = static_cast<uint64_t>(clock64());
+        t->end_ns = global_ns();
+        t->sm = sm_id();
+        t->reserved = 0;
+    }
 }
 
 // Many frames in one persistent launch.  The rays of all frames form one

@@ -101,6 +101,7 @@ struct RayParams {
     float* raydepth;
     rle_hit* rayhit;
     rle_counters* counters;
+    rle_ray_time* ray_time;       // per-ray start/end times (single-frame kernel), or null
     // launch shape (0 = default): lanes cooperating on one ray, DDA steps
     // each lane claims per chunk, block size
     int lanes_per_ray;

@@ -40,6 +40,7 @@ struct Req {
     size_t words = 0;
     double pixels = 0;
     double submit_s = 0, launch_s = 0, done_s = 0;
+    double gpu_ms = 0;  // device time of the request's batch (events around its launches)
     rle_status status = RLE_OK;
     int state = kQueued;
 };
@@ -47,7 +48,8 @@ struct Req {
 struct Slot {
     rle_batch* batch = nullptr;
     cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr;  // recorded before a batch's launches
+    cudaEvent_t done = nullptr;   // and after them
     bool busy = false;
     std::vector<uint64_t> tickets;
     void* workspace = nullptr;  // plain mode
@@ -91,6 +93,7 @@ void finish(rle_server* s, Req& q, rle_status st, double t) {
     c.submit_s = q.submit_s;
     c.launch_s = q.launch_s;
     c.done_s = t;
+    c.gpu_ms = q.gpu_ms;
     s->completions.push_back(c);
     if (st == RLE_OK) {
         s->completed++;
@@ -114,9 +117,14 @@ bool retire(rle_server* s) {
         const double t = now_s();
         const rle_status st = e == cudaSuccess ? RLE_OK : RLE_ERR_CUDA;
         if (e != cudaSuccess) rle::set_error("server: batch failed on the device: %s", cudaGetErrorString(e));
+        float gpu_ms = 0;
+        if (e == cudaSuccess && cudaEventElapsedTime(&gpu_ms, sl.start, sl.done) != cudaSuccess) gpu_ms = 0;
         for (uint64_t tk : sl.tickets) {
             auto it = s->reqs.find(tk);
-            if (it != s->reqs.end()) finish(s, it->second, st, t);
+            if (it != s->reqs.end()) {
+                it->second.gpu_ms = gpu_ms;
+                finish(s, it->second, st, t);
+            }
         }
         sl.tickets.clear();
         sl.busy = false;
@@ -176,7 +184,10 @@ bool launch_one(rle_server* s, std::unique_lock<std::mutex>& lk) {
     s->batches++;
     lk.unlock();
     rle_status st = RLE_OK;
-    if (inject) {
+    if (!inject && cudaEventRecord(slot->start, slot->stream) != cudaSuccess) st = RLE_ERR_CUDA;
+    if (st != RLE_OK) {
+        rle::set_error("server: cudaEventRecord failed");
+    } else if (inject) {
         rle::set_error("server: injected launch failure");
         st = RLE_ERR_CUDA;
     } else if (s->cfg.plain) {
@@ -237,6 +248,7 @@ void release(rle_server* s) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.batch) rle_batch_free(sl.batch);
         if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.start) cudaEventDestroy(sl.start);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.workspace) cudaFree(sl.workspace);
     }
@@ -286,7 +298,7 @@ extern "C" rle_status rle_server_create(const rle_server_config* cfg, rle_server
     for (Slot& sl : s->slots) {
         if (st != RLE_OK) break;
         if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventCreate(&sl.start) != cudaSuccess || cudaEventCreate(&sl.done) != cudaSuccess) {
             st = RLE_ERR_CUDA;
             break;
         }
@@ -389,6 +401,7 @@ extern "C" rle_status rle_server_wait(rle_server* s, uint64_t ticket, int timeou
         out->submit_s = it->second.submit_s;
         out->launch_s = it->second.launch_s;
         out->done_s = it->second.done_s;
+        out->gpu_ms = it->second.gpu_ms;
     }
     return RLE_OK;
 }

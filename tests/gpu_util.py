@@ -75,3 +75,35 @@ def assert_rays_equal(gpu, orc, label=""):
     assert dbad == 0, f"{label}: {dbad} depths differ"
     if gh is not None and oh is not None:
         assert np.array_equal(gh, oh), f"{label}: {int((gh != oh).sum())} hit records differ"
+
+
+def oracle_screen(po, rle, oscene, cam, view, hits: bool = True, nthreads: int = 0):
+    """The oracle's screen for one camera and view: the oracle's own ray map
+    (built from the camera and the view's resolved sizes), the oracle's
+    Render::render_line restatement and its resolve -- no product code on
+    the path but the call that resolves the view's defaults (maxres,
+    samples, distances), whose ray map must then equal the oracle's.
+    Returns (colour u32, depth f32, hits or None)."""
+    rm = rle.raymap_build(cam, view)
+    om = po.raymap_build(list(cam.pos), list(cam.rot), rm.border, rm.maxres, rm.fov_scale, rm.samples,
+                         rm.mip_distance, rm.z_far)
+    assert list(om.res) == list(rm.res), "oracle and product ray maps disagree on the fan sizes"
+    out, dep, hit, _ = po.render_rays(om, oscene, want_hits=hits, nthreads=nthreads)
+    col, d, h, _ = po.resolve(om, view.width, view.height, out, dep, hit)
+    return col, d, h
+
+
+def assert_screen_equal(got, want, label=""):
+    """Screen colour and hit records bit for bit; depth bit for bit with NaN
+    meeting NaN (the stated bar for depth is 1e-5 relative; the renderer
+    meets it with zero error)."""
+    gc, gd, gh = got
+    wc, wd, wh = want
+    assert gc.shape == wc.shape, label
+    bad = int((gc != wc).sum())
+    assert bad == 0, f"{label}: {bad} of {gc.size} pixels differ from the oracle"
+    dbad = int((float_bits(gd) != float_bits(wd)).sum())
+    assert dbad == 0, f"{label}: {dbad} depths differ from the oracle"
+    if gh is not None and wh is not None:
+        hbad = int((gh != wh).sum())
+        assert hbad == 0, f"{label}: {hbad} hit records differ from the oracle"

@@ -15,7 +15,8 @@ import os
 import numpy as np
 import pytest
 
-from gpu_util import Frame, assert_rays_equal, counters_dict, float_bits, oracle_counters
+from gpu_util import (Frame, assert_rays_equal, assert_screen_equal, counters_dict, float_bits, oracle_counters,
+                      oracle_screen)
 
 pytestmark = pytest.mark.gpu
 
@@ -86,8 +87,9 @@ def test_random_scene_view_camera(rle, po, torch_cuda, case):
 def test_random_batches(rle, po, torch_cuda, case):
     """Batches of 2-6 random views and cameras of one random scene, under a
     random launch shape (claim tile, lanes per ray, staging, graph or not,
-    one launch pair per frame or not), equal the frames rendered one by one:
-    colour, depth (NaN meeting NaN) and hit records."""
+    one launch pair per frame or not), equal the frames rendered one by one
+    and the oracle's screens: colour, depth (NaN meeting NaN) and hit
+    records."""
     torch = torch_cuda
     rng = np.random.default_rng(7000 + case)
     scene, oscene, n, sy = _scene(rle, po, rng)
@@ -122,5 +124,8 @@ def test_random_batches(rle, po, torch_cuda, case):
         assert torch.equal(outs[k][0], c), label
         assert np.array_equal(float_bits(outs[k][1].cpu().numpy()), float_bits(d.cpu().numpy())), label
         assert torch.equal(outs[k][2], h), label
+        got = (outs[k][0].cpu().numpy().view(np.uint32), outs[k][1].cpu().numpy(),
+               outs[k][2].cpu().numpy().view(rle.HIT_DTYPE))
+        assert_screen_equal(got, oracle_screen(po, rle, oscene, cam, view), label + " vs oracle")
     b.free()
     scene.free()

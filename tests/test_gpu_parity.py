@@ -240,3 +240,34 @@ def test_degenerate_scenes(rle, po, torch_cuda):
         orc, _ = _oracle_frame(po, rm, oscene)
         assert_rays_equal(gpu, orc, "degenerate")
         scene.free()
+
+
+def test_timed_launch_same_rays_and_sane_times(rle, po, caves256, torch_cuda):
+    """rle_render_rays_timed: the same ray buffer as the plain launch and
+    the oracle, and one time record per cast ray (end after start on the
+    SM's clock and on the device-wide clock, SM index below the SM count,
+    every ray inside the launch's span)."""
+    torch = torch_cuda
+    scene, oscene, _ = caves256
+    t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
+    g = rle.ground_height(t0, s0, 256, 256, 40, 200)
+    cam = rle.camera(40.5, 200.5, g + 30.0, 70.0, -12.0)
+    rm = rle.raymap_build(cam, rle.view_params(480, 270, mip_distance=96))
+    words = rle.raybuf_words(rm)
+    raybuf = torch.empty(words, dtype=torch.int32, device="cuda")
+    raydepth = torch.empty(words, dtype=torch.float32, device="cuda")
+    times = torch.zeros(rm.rays * rle.RAY_TIME_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    rle.render_rays_timed(scene, rm, raybuf, raydepth, times)
+    torch.cuda.synchronize()
+    n = rm.rays * rm.samples
+    got = (raybuf[:n].cpu().numpy().view(np.uint32), raydepth[:n].cpu().numpy(), None, None)
+    orc, _ = _oracle_frame(po, rm, oscene)
+    assert_rays_equal(got, orc, "timed launch")
+    t = times.cpu().numpy().view(rle.RAY_TIME_DTYPE)
+    assert t.size == rm.rays
+    assert (t["end_clock"] >= t["start_clock"]).all() and (t["end_ns"] >= t["start_ns"]).all()
+    assert (t["start_ns"] > 0).all()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert (t["sm"] < sms).all()
+    span_ns = int(t["end_ns"].max() - t["start_ns"].min())
+    assert 0 < span_ns < 10_000_000_000

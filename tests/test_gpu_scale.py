@@ -5,16 +5,27 @@
 - config 5: the 8192^2 x 512 scene built on the GPU, copied level by level
   to the host for the oracle, and a 3840x2160, 75 degree frame with mip
   switches at 256/512/1024 compared ray by ray (words, depths, hit records);
-- the batched launch at config-5 size equals the plain launches.
+- the batched launch at config-5 size equals the plain launches and the
+  oracle's screens.
 """
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from gpu_util import Frame, assert_rays_equal, float_bits
+from gpu_util import Frame, assert_rays_equal, assert_screen_equal, float_bits, oracle_screen
 
 pytestmark = pytest.mark.gpu
+
+
+def _bench():
+    import sys
+    from pathlib import Path
+    root = str(Path(__file__).resolve().parents[1])
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    return bench
 
 
 def _poses(rle, table, words, sx, sy, sz, n, seed, lo, hi, fov):
@@ -51,7 +62,7 @@ def test_config2_full_frames(rle, po, torch_cuda):
 
 @pytest.fixture(scope="module")
 def config5(rle, po, torch_cuda):
-    p = rle.scenegen_default(8192, 512, 8192, 7, caves=True)
+    p = _bench().dense_caves_8192(rle, 7)  # the benchmark's large scene, ~12 runs per column
     scene = rle.Scene.generate_on_device(p)
     info = scene.info()
     levels = []
@@ -79,7 +90,9 @@ def test_config5_4k_frame(rle, po, torch_cuda, config5):
         assert_rays_equal(gpu, orc, f"4K pose {k}")
 
 
-def test_config5_batched_equals_plain(rle, torch_cuda, config5):
+def test_config5_batched_equals_plain(rle, po, torch_cuda, config5):
+    """Four 4K views of the large scene in one batch: each equals the plain
+    launch and the oracle's screen."""
     torch = torch_cuda
     scene, oscene = config5
     t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
@@ -100,4 +113,6 @@ def test_config5_batched_equals_plain(rle, torch_cuda, config5):
         torch.cuda.synchronize()
         assert torch.equal(c, outs[k][0]), f"frame {k} colour"
         assert torch.equal(d.view(torch.int32), outs[k][1].view(torch.int32)), f"frame {k} depth"
+        got = (outs[k][0].cpu().numpy().view(np.uint32), outs[k][1].cpu().numpy(), None)
+        assert_screen_equal(got, oracle_screen(po, rle, oscene, cam, view, hits=False), f"4K batch frame {k}")
     b.free()

@@ -1,7 +1,9 @@
 """Render server (rle_server_*): continuous batching over resident scenes.
 
 - every result served in a mixed stream equals the same request rendered
-  alone (bit for bit), for the batching and the plain server;
+  alone and the oracle's screen for it (bit for bit), for the batching and
+  the plain server, at test sizes and in a config-4 mix (two resident
+  scenes of different sizes, resolutions up to 1920x1080);
 - admission: budgets and per-request limits refuse cleanly;
 - failure handling without any device fault: cancelled requests, bounded
   waits that time out, and injected launch failures (host side) that fail
@@ -12,20 +14,27 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from gpu_util import assert_screen_equal, oracle_screen
+
 pytestmark = pytest.mark.gpu
 
 RES = [(256, 256), (640, 480), (320, 240), (400, 300)]
 
 
 @pytest.fixture(scope="module")
-def scenes(rle, torch_cuda):
+def scene_pairs(rle, po, torch_cuda):
     out = []
     for n, seed in ((256, 3), (128, 4)):
         data = rle.scenegen_rle4(rle.scenegen_default(n, 256, n, seed, caves=True))
-        out.append(rle.Scene.from_bytes(data))
+        out.append((rle.Scene.from_bytes(data), po.OracleScene.from_rle4(data)))
     yield out
-    for s in out:
+    for s, _ in out:
         s.free()
+
+
+@pytest.fixture(scope="module")
+def scenes(scene_pairs):
+    return [s for s, _ in scene_pairs]
 
 
 def _requests(rle, scenes, n, seed):
@@ -62,8 +71,9 @@ def _alone(rle, torch, scene, cam, view):
 
 
 @pytest.mark.parametrize("plain", [False, True])
-def test_served_results_equal_alone(rle, scenes, torch_cuda, plain):
+def test_served_results_equal_alone(rle, po, scene_pairs, torch_cuda, plain):
     torch = torch_cuda
+    scenes = [s for s, _ in scene_pairs]
     srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
                      max_samples=640, plain=plain)
     ids = [srv.add_scene(s) for s in scenes]
@@ -79,8 +89,11 @@ def test_served_results_equal_alone(rle, scenes, torch_cuda, plain):
     torch.cuda.synchronize()
     for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
         wc, wd = _alone(rle, torch, scenes[sid], cam, view)
-        assert np.array_equal(c.cpu().numpy().view(np.uint32), wc), f"request {i} colour"
-        assert np.array_equal(d.cpu().numpy().view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+        gc, gd = c.cpu().numpy().view(np.uint32), d.cpu().numpy()
+        assert np.array_equal(gc, wc), f"request {i} colour"
+        assert np.array_equal(gd.view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+        orc = oracle_screen(po, rle, scene_pairs[sid][1], cam, view, hits=False)
+        assert_screen_equal((gc, gd, None), orc, f"request {i} (scene {sid}, {view.width}x{view.height}) vs oracle")
     st = srv.stats()
     assert st.completed == 24 and st.failed == 0
     assert st.p99_ms >= st.p50_ms > 0 and st.mrays_per_s > 0
@@ -90,6 +103,9 @@ def test_served_results_equal_alone(rle, scenes, torch_cuda, plain):
         assert st.batches < 24  # requests were batched
     done = srv.poll()
     assert sorted(c.ticket for c in done) == sorted(tickets)
+    # every completion carries its launch's device time, within its host span
+    for c in done:
+        assert 0 < c.gpu_ms <= (c.done_s - c.submit_s) * 1e3 + 1.0
     srv.destroy()
 
 
@@ -167,11 +183,13 @@ def test_cancel_timeout_and_injected_failures(rle, scenes, torch_cuda):
     srv.destroy()
 
 
-def test_concurrent_submitters(rle, scenes, torch_cuda):
+def test_concurrent_submitters(rle, po, scene_pairs, torch_cuda):
     """Four host threads submit and wait at once; every result equals the
-    request rendered alone and every ticket completes exactly once."""
+    request rendered alone and the oracle's screen, and every ticket
+    completes exactly once."""
     import threading
     torch = torch_cuda
+    scenes = [s for s, _ in scene_pairs]
     srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
                      max_samples=640)
     for s in scenes:
@@ -205,8 +223,73 @@ def test_concurrent_submitters(rle, scenes, torch_cuda):
     torch.cuda.synchronize()
     for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
         wc, wd = _alone(rle, torch, scenes[sid], cam, view)
-        assert np.array_equal(c.cpu().numpy().view(np.uint32), wc), f"request {i} colour"
-        assert np.array_equal(d.cpu().numpy().view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+        gc, gd = c.cpu().numpy().view(np.uint32), d.cpu().numpy()
+        assert np.array_equal(gc, wc), f"request {i} colour"
+        assert np.array_equal(gd.view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+        orc = oracle_screen(po, rle, scene_pairs[sid][1], cam, view, hits=False)
+        assert_screen_equal((gc, gd, None), orc, f"request {i} vs oracle")
     st = srv.stats()
     assert st.submitted == 32 and st.completed == 32 and st.failed == 0
     srv.destroy()
+
+
+SERVE_RES = [((256, 256), 0.4), ((640, 480), 0.3), ((1280, 720), 0.2), ((1920, 1080), 0.1)]
+
+
+def _pow2_ceil(v):
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
+
+
+@pytest.mark.parametrize("plain", [False, True])
+def test_config4_mix_against_oracle(rle, po, torch_cuda, plain):
+    """A config-4 served mix: two resident cave scenes of different sizes
+    (1024^2 and 2048^2 x 256, seeds 3 and 4), 40 requests with the config's
+    resolution law (256x256 .4, 640x480 .3, 1280x720 .2, 1920x1080 .1; every
+    resolution at least once) and config-2 poses, submitted at once so that
+    they batch; every served frame equals the oracle's screen and the
+    request rendered alone."""
+    torch = torch_cuda
+    pairs = []
+    for n, seed in ((1024, 3), (2048, 4)):
+        data = rle.scenegen_rle4(rle.scenegen_default(n, 256, n, seed, caves=True))
+        pairs.append((rle.Scene.from_bytes(data), po.OracleScene.from_rle4(data), n))
+    srv = rle.Server(hbm_budget_bytes=16 << 30, raybuf_words=32 << 20, max_frames_per_batch=16, max_inflight=3,
+                     max_samples=2048, plain=plain)
+    for s, _, _ in pairs:
+        srv.add_scene(s)
+    rng = np.random.default_rng(20261205)
+    probs = np.array([p for _, p in SERVE_RES])
+    reqs = []
+    for i in range(40):
+        sid = i % 2 if i < 8 else int(rng.integers(0, 2))
+        w, h = SERVE_RES[i % 4][0] if i < 8 else SERVE_RES[int(rng.choice(4, p=probs))][0]
+        _, osc, n = pairs[sid]
+        t0, s0 = osc.levels[0][3], osc.levels[0][4]
+        x, z = rng.uniform(0, n, 2)
+        g = rle.ground_height(t0, s0, n, 256, int(x), int(z))
+        cam = rle.camera(float(x), float(z), g + float(rng.uniform(10, 80)), float(rng.uniform(0, 360)),
+                         float(rng.uniform(1, 30) * rng.choice([-1, 1])))
+        reqs.append((sid, cam, rle.view_params(w, h, samples=_pow2_ceil(w))))
+    bufs = _buffers(torch, reqs)
+    tickets = [srv.submit(sid, cam, view, c, d) for (sid, cam, view), (c, d) in zip(reqs, bufs)]
+    for t in tickets:
+        assert srv.wait(t, 60000).status == 0
+    srv.drain(60000)
+    torch.cuda.synchronize()
+    st = srv.stats()
+    assert st.completed == 40 and st.failed == 0
+    if not plain:
+        assert st.batches < 40
+    for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
+        gc, gd = c.cpu().numpy().view(np.uint32), d.cpu().numpy()
+        label = f"request {i} (scene {sid}, {view.width}x{view.height}, {'plain' if plain else 'batched'})"
+        assert_screen_equal((gc, gd, None), oracle_screen(po, rle, pairs[sid][1], cam, view, hits=False),
+                            label + " vs oracle")
+        wc, wd = _alone(rle, torch, pairs[sid][0], cam, view)
+        assert np.array_equal(gc, wc) and np.array_equal(gd.view(np.uint32), wd.view(np.uint32)), label
+    srv.destroy()
+    for s, _, _ in pairs:
+        s.free()

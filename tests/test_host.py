@@ -113,6 +113,7 @@ def test_invalid_arguments_return_status(rle):
         rle.scenegen_rle4(p)
     lib = rle.library()
     assert lib.rle_render_rays(None, None, None, None, None, None, None) == -1
+    assert lib.rle_render_rays_timed(None, None, None, None, None, None) == -1
     h = C.c_void_p()
     assert lib.rle_scene_load_memory(b"\x01\x00", 2, 0, C.byref(h)) == -3  # truncated header
     assert lib.rle_scene_load_file(b"/nonexistent.rle4", 0, C.byref(h)) == -2

@@ -205,3 +205,78 @@ def test_raycast_matches_reference_random(po, seed):
         diff += int((out != ref).sum())
     assert total > 0
     assert diff == 0, f"{diff} of {total} samples differ"
+
+
+# ---------------------------------------------------------------------------
+# at the benchmark's sizes: the 2048^2 cave scene, 1080p and 4K frames
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def cave2048(po):
+    """The 2048^2 x 256 cave scene (seed 2) of the plain-frame benchmark,
+    made by the library's host generator."""
+    from conftest import ensure_built, load_package
+    ensure_built()
+    rle = load_package()
+    data = rle.scenegen_rle4(rle.scenegen_default(2048, 256, 2048, 2, caves=True))
+    return rle, po.OracleScene.from_rle4(data)
+
+
+def _bench_poses(rle, oscene, count, seed, lo, hi, fov=90.0):
+    """Cameras by the benchmark's law: uniform over the grid, lo-hi voxels
+    above the local ground, yaw U[0,360), pitch +-U[1,30]."""
+    sx, sy = oscene.levels[0][0], oscene.levels[0][1]
+    t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(count):
+        x, z = rng.uniform(0, sx), rng.uniform(0, sx)
+        g = rle.ground_height(t0, s0, sx, sy, int(x), int(z))
+        pitch = float(rng.uniform(1.0, 30.0) * rng.choice([-1.0, 1.0]))
+        cams.append(rle.camera(float(x), float(z), g + float(rng.uniform(lo, hi)), float(rng.uniform(0, 360)),
+                               pitch, fov, scene_height=sy))
+    return cams
+
+
+def _pin_frame(po, rle, oscene, cam, view, label):
+    rm = rle.raymap_build(cam, view)
+    om = po.raymap_build(list(cam.pos), list(cam.rot), rm.border, rm.maxres, 1.0, rm.samples, rm.mip_distance,
+                         rm.z_far)
+    rb = po.ref_raymap(list(cam.pos), list(cam.rot), rm.border, rm.maxres)
+    f = po.ref_raymap_fields(rb)
+    assert list(om.res) == list(f["res"]), label
+    assert np.array_equal(np.array(list(om.to3d), np.float32).view(np.uint32), f["to3d"].ravel().view(np.uint32))
+    nr = po.rays_to_render(om)
+    ref = po.ref_render_rays(rb, oscene, rm.samples, nr, rm.mip_distance, rm.z_far)
+    out, _, _, _ = po.render_rays(om, oscene)
+    assert out.size == nr * rm.samples and nr > 1000, label
+    diff = int((out != ref).sum())
+    assert diff == 0, f"{label}: {diff} of {out.size} samples differ from the reference"
+    # the frame reaches the sizes it is here for: samples in mask word 31 and
+    # beyond (y >= 992) drawn, long rows
+    drawn = (out.reshape(nr, rm.samples) != 0) & (((out.reshape(nr, rm.samples) >> 16) & 0xFF) != 0xFF)
+    assert drawn[:, 992:].any(), label
+
+
+@needs_ref
+@pytest.mark.parametrize("k", range(3))
+def test_config2_frames_match_reference(po, cave2048, k):
+    """Three poses of the benchmark's camera path (seed 20261203) on its
+    2048^2 cave scene at 1920x1080, 2048 samples per column ray: the
+    oracle's ray buffer equals the reference's Render::render_line build."""
+    rle, oscene = cave2048
+    cam = _bench_poses(rle, oscene, 3, 20261203, 10, 80)[k]
+    _pin_frame(po, rle, oscene, cam, rle.view_params(1920, 1080, samples=2048), f"config-2 pose {k}")
+
+
+@needs_ref
+@pytest.mark.parametrize("k", range(2))
+def test_4k_frames_match_reference(po, cave2048, k):
+    """3840x2160 frames, 4096 samples per column ray, level switches at
+    256/512/1024 voxels (the 4K benchmark's LOD law), cameras 20-200 above
+    the ground, on the 2048^2 cave scene (its slabs fit the harness's
+    below-4-GiB placement); 90 degrees, the reference's fixed frustum."""
+    rle, oscene = cave2048
+    cam = _bench_poses(rle, oscene, 2, 7, 20, 200)[k]
+    _pin_frame(po, rle, oscene, cam, rle.view_params(3840, 2160, samples=4096, mip_distance=256),
+               f"4K pose {k}")

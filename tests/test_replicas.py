@@ -76,3 +76,25 @@ def test_ranks_render_distinct_camera_paths(rle):
     a = bench.poses(rle, (sx, sy, sz, table, words), 4, seed=20261203 + 0)
     b = bench.poses(rle, (sx, sy, sz, table, words), 4, seed=20261203 + 1)
     assert not np.allclose([c.pos[0] for c in a], [c.pos[0] for c in b])
+
+
+def test_gpus_flag_starts_that_many_ranks():
+    """`bench.py --gpus 2` started without a launcher starts two ranks
+    itself (RANK / WORLD_SIZE set as torch.distributed.run sets them); here
+    in its host-only plan mode over gloo: both ranks join, their camera
+    paths differ, and the reduced work is both ranks' pixels.  A --gpus
+    that disagrees with an outer launcher's WORLD_SIZE is refused."""
+    import json
+    import subprocess
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--plan-only", "--backend", "gloo",
+                        "--steps", "4", "--warmup", "3", "--plan-scene", "128"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["n_gpus"] == 2
+    assert len(line["camera_paths"]) == 2 and line["camera_paths"][0] != line["camera_paths"][1]
+    assert line["pixels_all_ranks"] == 2 * 4 * 1920 * 1080
+    bad = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--plan-only"],
+                         capture_output=True, text=True, timeout=120, cwd=ROOT, env=dict(env, WORLD_SIZE="3"))
+    assert bad.returncode != 0 and "WORLD_SIZE" in bad.stderr

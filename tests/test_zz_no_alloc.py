@@ -83,3 +83,33 @@ def test_noalloc_refuses_frames_beyond_its_buffer(rle, scene, torch_cuda):
     with pytest.raises(rle.RLEError) as e:
         rle.render_frame_noalloc(scene, cam, view, colour, depth)
     assert e.value.name == "RLE_ERR_CAPACITY"
+
+
+def test_noalloc_calls_after_the_first_allocate_nothing(rle, scene, torch_cuda):
+    """The property the entry point exists for: once the first call on the
+    device has reserved the built-in array (and loaded the kernels), further
+    calls leave the device's free memory exactly as it was -- no cudaMalloc,
+    no allocating library routine -- and their pictures still equal
+    rle_render_frame's."""
+    torch = torch_cuda
+    info = scene.info()
+    table, words = scene.copy_level(0)
+    view = rle.view_params(480, 270)
+    g = rle.ground_height(table, words, info.sx[0], info.sy[0], 120, 130)
+    cam = rle.camera(120.5, 130.5, g + 25.0, 140.0, -18.0)
+    want_c, want_d = _with_workspace(rle, torch, scene, cam, view)
+    n = view.width * view.height
+    colour = torch.empty(n, dtype=torch.int32, device="cuda")
+    depth = torch.empty(n, dtype=torch.float32, device="cuda")
+    lib = rle.library()
+    call = lambda: lib.rle_render_frame_noalloc(scene.handle, C.byref(cam), C.byref(view),  # noqa: E731
+                                                colour.data_ptr(), depth.data_ptr(), None)
+    assert call() == 0, lib.rle_last_error()  # the first call may reserve the array
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        assert call() == 0, lib.rle_last_error()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(colour.cpu().numpy().view(np.uint32), want_c)
+    assert np.array_equal(depth.cpu().numpy().view(np.uint32), want_d.view(np.uint32))
