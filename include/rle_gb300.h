@@ -258,11 +258,17 @@ typedef struct rle_counters {
  *   lanes_per_ray      lanes of a warp cooperating on one column ray: 8, 16
  *                      or 32 (4, 2 or 1 rays per warp); default 32
  *   cells_per_lane     DDA steps each lane takes per chunk: 1 (reserved)
- *   threads_per_block  32, 64, 96 or 128; default 128 */
+ *   threads_per_block  32, 64, 96 or 128; default 128
+ *   staging            staging depth of the column data a ray reads: 1 the
+ *                      column-table entries of the next chunk of cells load
+ *                      while the current chunk is merged; 2 also each of
+ *                      those cells' run-header line is staged in L2 before
+ *                      its scan; 3 the same into L1; default 1 */
 typedef struct rle_tuning {
     int lanes_per_ray;
     int cells_per_lane;
     int threads_per_block;
+    int staging;
 } rle_tuning;
 rle_status rle_tuning_set(const rle_tuning* t);
 rle_status rle_tuning_get(rle_tuning* t);
@@ -341,10 +347,10 @@ typedef struct rle_frame_request {
 } rle_frame_request;
 
 typedef struct rle_batch_tuning {
-    int tile_rays;          /* most rays a lane group claims at once: 1..256 (default 1;
-                               claims shrink further as the queue drains) */
+    int tile_rays;          /* tile width: most adjacent column rays a lane group claims at
+                               once, 1..256 (default 1; claims shrink as the queue drains) */
     int lanes_per_ray;      /* lanes cooperating on one column ray: 8, 16, 32 */
-    int staging;            /* staging depth: tiles a lane group claims per grab, 1..8 */
+    int staging;            /* staging depth of the column data, 1..3, as rle_tuning.staging */
     int threads_per_block;  /* 32, 64, 96 or 128 */
     int use_graph;          /* 1: capture once and replay (default); 0: plain launches */
     int per_frame;          /* 1: one plain raycast + resolve launch per frame instead of the
@@ -368,8 +374,9 @@ size_t rle_batch_words_needed(const rle_frame_request* frames, int n);
 rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                             void* stream);
 /* Times every tile_rays x lanes_per_ray x staging combination
- * ({1,2,4,8,16,32,64} x {8,16,32} x {1,2,3}) and the per-frame launches (lanes
- * {8,16,32}) on these frames (median of `repeats`
+ * ({1,2,4,8,16,32,64} x {8,16,32} x {1,2,3}: tile width, 4/2/1 rays per
+ * warp, staging depth -- three independent axes) and the per-frame launches
+ * (lanes {8,16,32} x staging {1,2,3}) on these frames (median of `repeats`
  * runs each), keeps the fastest as the batch's tuning and returns it. */
 rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, const rle_frame_request* frames, int n,
                               int repeats, rle_batch_tuning* best, float* best_ms);

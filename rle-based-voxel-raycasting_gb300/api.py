@@ -81,7 +81,8 @@ class Counters(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("lanes_per_ray", C.c_int), ("cells_per_lane", C.c_int), ("threads_per_block", C.c_int)]
+    _fields_ = [("lanes_per_ray", C.c_int), ("cells_per_lane", C.c_int), ("threads_per_block", C.c_int),
+                ("staging", C.c_int)]
 
 
 RAYCAST_SHAPES = [(8, 1), (16, 1), (32, 1)]
@@ -371,16 +372,17 @@ def raybuf_words(rm: RayMap) -> int:
     return int(_lib.rle_raybuf_words(C.byref(rm)))
 
 
-def tuning_set(lanes_per_ray: int = 0, cells_per_lane: int = 0, threads_per_block: int = 0) -> None:
+def tuning_set(lanes_per_ray: int = 0, cells_per_lane: int = 0, threads_per_block: int = 0, staging: int = 0) -> None:
     """Process-wide launch shape of the raycast (0 = built-in default)."""
-    _check(_lib.rle_tuning_set(C.byref(Tuning(lanes_per_ray, cells_per_lane, threads_per_block))),
+    _check(_lib.rle_tuning_set(C.byref(Tuning(lanes_per_ray, cells_per_lane, threads_per_block, staging))),
            "rle_tuning_set")
 
 
-def tuning_get() -> tuple[int, int, int]:
+def tuning_get() -> tuple[int, int, int, int]:
+    """(lanes_per_ray, cells_per_lane, threads_per_block, staging)."""
     t = Tuning()
     _check(_lib.rle_tuning_get(C.byref(t)), "rle_tuning_get")
-    return t.lanes_per_ray, t.cells_per_lane, t.threads_per_block
+    return t.lanes_per_ray, t.cells_per_lane, t.threads_per_block, t.staging
 
 
 # ---------------------------------------------------------------------------

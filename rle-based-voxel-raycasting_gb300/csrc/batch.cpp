@@ -35,7 +35,7 @@ struct Layout {
 bool valid_tuning(const rle_batch_tuning& t) {
     return t.tile_rays >= 1 && t.tile_rays <= 256 && (t.lanes_per_ray == 8 || t.lanes_per_ray == 16 ||
                                                       t.lanes_per_ray == 32) &&
-           t.staging >= 1 && t.staging <= 8 && t.threads_per_block >= 32 && t.threads_per_block <= 128 &&
+           t.staging >= 1 && t.staging <= 3 && t.threads_per_block >= 32 && t.threads_per_block <= 128 &&
            t.threads_per_block % 32 == 0 && (t.use_graph == 0 || t.use_graph == 1) &&
            (t.per_frame == 0 || t.per_frame == 1);
 }
@@ -235,6 +235,7 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
         for (int i = 0; i < n && st == RLE_OK; i++) {
             rp[i].lanes_per_ray = b->tuning.lanes_per_ray;
             rp[i].threads_per_block = b->tuning.threads_per_block;
+            rp[i].staging = b->tuning.staging;
             st = rle::launch_raycast(rp[i], stream);
             if (st == RLE_OK) st = rle::launch_resolve(sp[i], stream);
         }
@@ -341,7 +342,7 @@ extern "C" rle_status rle_batch_free(rle_batch* b) {
 
 extern "C" rle_status rle_batch_set_tuning(rle_batch* b, const rle_batch_tuning* t) {
     if (!b || !t || !valid_tuning(*t)) {
-        rle::set_error("rle_batch_set_tuning: tile 1..256, lanes 8/16/32, staging 1..8, threads 32..128 step 32");
+        rle::set_error("rle_batch_set_tuning: tile 1..256, lanes 8/16/32, staging 1..3, threads 32..128 step 32");
         return RLE_ERR_INVALID_ARG;
     }
     std::lock_guard<std::mutex> lock(b->mu);
@@ -425,7 +426,6 @@ extern "C" rle_status rle_batch_autotune(rle_batch* b, const rle_scene* scene, c
         // the persistent launch over tile x staging, then the per-frame launches (tile -1)
         for (int tv : {1, 2, 4, 8, 16, 32, 64, -1}) {
             for (int sv : stagings) {
-                if (tv < 0 && sv > 1) break;
                 rle_batch_tuning t = start;
                 t.per_frame = tv < 0 ? 1 : 0;
                 t.tile_rays = tv < 0 ? start.tile_rays : tv;

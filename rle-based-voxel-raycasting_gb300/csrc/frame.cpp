@@ -129,6 +129,7 @@ namespace {
 std::atomic<int> g_lanes_per_ray{0};
 std::atomic<int> g_cells_per_lane{0};
 std::atomic<int> g_threads_per_block{0};
+std::atomic<int> g_staging{0};
 
 bool shape_built(int lanes, int cells) {
     return (lanes == 0 || lanes == 8 || lanes == 16 || lanes == 32) && (cells == 0 || cells == 1);
@@ -137,14 +138,16 @@ bool shape_built(int lanes, int cells) {
 
 extern "C" rle_status rle_tuning_set(const rle_tuning* t) {
     if (!t) return RLE_ERR_INVALID_ARG;
-    const int l = t->lanes_per_ray, c = t->cells_per_lane, b = t->threads_per_block;
-    if (!shape_built(l, c) || b < 0 || b > 128 || b % 32 != 0) {
-        rle::set_error("rle_tuning_set: lanes_per_ray in {0,8,16,32}, cells_per_lane in {0,1}, threads_per_block in {0,32,..,128}");
+    const int l = t->lanes_per_ray, c = t->cells_per_lane, b = t->threads_per_block, st = t->staging;
+    if (!shape_built(l, c) || b < 0 || b > 128 || b % 32 != 0 || st < 0 || st > 3) {
+        rle::set_error("rle_tuning_set: lanes_per_ray in {0,8,16,32}, cells_per_lane in {0,1}, threads_per_block in "
+                       "{0,32,..,128}, staging in {0,1,2,3}");
         return RLE_ERR_INVALID_ARG;
     }
     g_lanes_per_ray = l;
     g_cells_per_lane = c;
     g_threads_per_block = b;
+    g_staging = st;
     return RLE_OK;
 }
 
@@ -153,6 +156,7 @@ extern "C" rle_status rle_tuning_get(rle_tuning* t) {
     t->lanes_per_ray = g_lanes_per_ray;
     t->cells_per_lane = g_cells_per_lane;
     t->threads_per_block = g_threads_per_block;
+    t->staging = g_staging;
     return RLE_OK;
 }
 
@@ -178,6 +182,7 @@ extern "C" rle_status rle_render_rays(const rle_scene* scene, const rle_raymap* 
     p.lanes_per_ray = g_lanes_per_ray;
     p.cells_per_lane = g_cells_per_lane;
     p.threads_per_block = g_threads_per_block;
+    p.staging = g_staging;
     rle::DeviceGuard g(scene->device);
     if (!g.ok) {
         rle::set_error("rle_render_rays: cannot select device %d", scene->device);
@@ -201,6 +206,7 @@ extern "C" rle_status rle_render_rays_timed(const rle_scene* scene, const rle_ra
     p.lanes_per_ray = g_lanes_per_ray;
     p.cells_per_lane = g_cells_per_lane;
     p.threads_per_block = g_threads_per_block;
+    p.staging = g_staging;
     rle::DeviceGuard g(scene->device);
     if (!g.ok) {
         rle::set_error("rle_render_rays_timed: cannot select device %d", scene->device);

@@ -107,6 +107,13 @@ __device__ __forceinline__ uint32_t sm_id() {
     return s;
 }
 
+// Run-header staging (the launch's staging depth): 2 stages a cell's header
+// line in L2, 3 in L1, ahead of the scan that reads it.
+__device__ __forceinline__ void stage_headers(const uint16_t* h, int staging) {
+    if (staging == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h));
+    else if (staging >= 3) asm volatile("prefetch.global.L1 [%0];" ::"l"(h));
+}
+
 // First lane of the group a lane mask describes.
 __device__ __forceinline__ int lane_base(unsigned gmask) { return __ffs(gmask) - 1; }
 
@@ -539,8 +546,18 @@ __device__ __forceinline__ void cell_geometry(const RayParams& P, const Ray& R, 
 // those tests.  The scan ends where the walk would already break at the
 // chunk's horizon.  More than kRecs such runs: c.nrec = -1, and the merge
 // walks the runs itself.
-__device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int ymin, int ymax, Cell& c,
-                                          float4* rec) {
+//
+// A run none of whose samples in the open range [ymin, ymax) is still free
+// in the occupancy mask is dropped the same way (its scr_y2 folded into the
+// next record's guard).  Its turn in the walk could not colour a sample
+// either: the mask only gains bits and the range only closes.  Nor can it
+// move the horizon in a way that matters: ymin always names a free sample
+// (or the range is closed), so a span with no free sample never reaches
+// ymin, and the ymax it would set only cuts off samples that are all taken
+// -- ymin, the only horizon value the walk's other tests read, evolves the
+// same with or without it.
+__device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, const Mask& mask, int ymin, int ymax,
+                                          Cell& c, float4* rec) {
     const float res_y2 = static_cast<float>(P.S / 2);
     const float mountain = P.posy;
     const int mip = c.mip;
@@ -584,6 +601,11 @@ __device__ __forceinline__ bool scan_runs(const RayParams& P, const Ray& R, int 
         const float py2 = cyy2 + R.pos3d_y_add * sgf;
         const int scr_y1 = static_cast<int>(res_y2 + py2 / pz2 - 1);
         if (scr_y1 >= ymax) continue;
+        {  // every sample it could colour is taken already
+            const int lo = scr_y1 > ymin ? scr_y1 : ymin;
+            const int hi = scr_y2 < ymax ? scr_y2 : ymax;
+            if (mask.first_clear(lo, hi) >= hi) continue;
+        }
         if (n == kRecs) {
             n = -1;
             break;
@@ -896,7 +918,7 @@ __device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, fl
 // chunks of G DDA steps, lane k taking step k of each.
 template <int G, bool kCount, bool kHits, bool kDefer>
 __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, float4* recs,
-                                         float4* spans, int k, unsigned gmask, Counts& cnt) {
+                                         float4* spans, int k, unsigned gmask, int staging, Counts& cnt) {
     const int S = P.S;
     const int words = (S + 31) >> 5;
     Mask mask{mask_words};
@@ -967,7 +989,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             }
 
             // ---- 2. each lane: its cell -- pre-cull at the current horizon, run scan ----
-            const bool drawable = scan_runs(P, R, ymin, ymax, c, my_recs);
+            const bool drawable = scan_runs(P, R, mask, ymin, ymax, c, my_recs);
             // with counters every valid cell goes through the exact walk
             unsigned todo = __ballot_sync(gmask, kCount ? valid : drawable) >> lane_base(gmask);
             if constexpr (G < 32) todo &= (1u << G) - 1u;
@@ -1029,6 +1051,12 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             // reference walks on to z_far without drawing).  Exact counters
             // need the full walk, so they keep it.
             if (done_next) break;
+            // staging depth >= 2: the next chunk's table entries have arrived
+            // under the merge; stage each cell's header line (second header
+            // on; the first travels in the table entry) for its scan, which
+            // follows the next DDA chunk
+            if (staging >= 2 && c_next.loaded && (c_next.ey & 0xffffu) > 1u)
+                stage_headers(P.slabs[c_next.mip] + 3 + c_next.ex, staging);
             c = c_next;
             nvalid = nvalid_next;
         }
@@ -1110,7 +1138,8 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
         t->start_ns = global_ns();
         t->start_clock = static_cast<uint64_t>(clock64());
     }
-    cast_ray<G, kCount, kHits, kDefer>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, cnt);
+    cast_ray<G, kCount, kHits, kDefer>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, P.staging,
+                                       cnt);
     if (P.ray_time && L.k == 0 && x < P.rays) {
         rle_ray_time* t = P.ray_time + x;
         t->end_clock = static_cast<uint64_t>(clock64());
@@ -1140,10 +1169,10 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                : nullptr;
     Counts cnt;
     int f = 0;  // frame of the current ray (rays are taken in increasing order)
-    // Guided self-scheduling: a group claims up to tile * staging rays, but
+    // Guided self-scheduling: a group claims up to `tile` adjacent rays, but
     // never more than half its fair share of what is left, so the last rays
     // go out one at a time and no group is left with a long private tail.
-    const int grab = tile * staging;
+    const int grab = tile;
     const int groups = static_cast<int>(gridDim.x) * (static_cast<int>(blockDim.x) / G);
     for (;;) {
         unsigned int t0 = 0, n = 1;
@@ -1167,7 +1196,7 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 f = lo;
             }
             cast_ray<G, false, kHits, kDefer>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k, L.gmask,
-                                             cnt);
+                                             staging, cnt);
         }
     }
 }
@@ -1286,8 +1315,8 @@ rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits,
 }
 
 rle_status launch_raycast_batch(const BatchRaycast& b, void* stream) {
-    if (b.threads % 32 != 0 || b.threads <= 0 || b.threads > 128 || b.tile < 1 || b.staging < 1) {
-        set_error("batch: threads per block a multiple of 32 up to 128, tile >= 1, staging >= 1");
+    if (b.threads % 32 != 0 || b.threads <= 0 || b.threads > 128 || b.tile < 1 || b.staging < 1 || b.staging > 3) {
+        set_error("batch: threads per block a multiple of 32 up to 128, tile >= 1, staging 1..3");
         return RLE_ERR_INVALID_ARG;
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1324,6 +1353,10 @@ rle_status launch_raycast(const RayParams& p, void* stream) {
     const int threads = p.threads_per_block > 0 ? p.threads_per_block : 128;
     if (threads % 32 != 0 || threads > 128) {
         set_error("raycast: threads per block must be a multiple of 32, at most 128");
+        return RLE_ERR_INVALID_ARG;
+    }
+    if (p.staging < 0 || p.staging > 3) {
+        set_error("raycast: staging depth 1..3 (0 = default)");
         return RLE_ERR_INVALID_ARG;
     }
     switch (lanes) {

@@ -107,6 +107,7 @@ struct RayParams {
     int lanes_per_ray;
     int cells_per_lane;
     int threads_per_block;
+    int staging;                  // staging depth of the column data (1..3; 0 = default)
 };
 
 // Per-frame constants of the resolve (uniforms of colorize_buddha_soft.frag).
@@ -146,8 +147,8 @@ struct BatchRaycast {
     BatchHeader* header;       // device
     const int* ray_start;      // device array [nframes + 1], prefix of rays
     const RayParams* frames;   // device array [nframes]
-    int tile;                  // rays per tile
-    int staging;               // tiles a group claims per grab
+    int tile;                  // most adjacent rays a lane group claims at once
+    int staging;               // staging depth of the column data (1..3)
     int lanes;                 // lanes per ray: 8, 16, 32
     int threads;               // block size
     int max_samples;           // largest S of the frames the launch may see

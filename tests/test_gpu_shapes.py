@@ -1,6 +1,6 @@
-"""Every launch shape of the raycast (lanes per ray x block size) gives the
-same bits: ray buffer, depths, hit records and work counters equal the
-oracle's for a plain terrain and a cave scene."""
+"""Every launch shape of the raycast (lanes per ray x block size x staging
+depth) gives the same bits: ray buffer, depths, hit records and work
+counters equal the oracle's for a plain terrain and a cave scene."""
 from __future__ import annotations
 
 import numpy as np
@@ -18,18 +18,18 @@ def scenes(rle, po, torch_cuda):
         data = rle.scenegen_rle4(rle.scenegen_default(n, 256, n, seed, caves=caves))
         out.append((rle.Scene.from_bytes(data), po.OracleScene.from_rle4(data)))
     yield out
-    rle.tuning_set(0, 0, 0)
+    rle.tuning_set(0, 0, 0, 0)
 
 
 SHAPES = [(8, 1), (16, 1), (32, 1)]
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-@pytest.mark.parametrize("threads", [32, 128])
-def test_shapes_bit_exact(rle, po, scenes, torch_cuda, shape, threads):
+@pytest.mark.parametrize("threads,staging", [(32, 1), (128, 1), (128, 2), (64, 3)])
+def test_shapes_bit_exact(rle, po, scenes, torch_cuda, shape, threads, staging):
     lanes, cells = shape
-    rle.tuning_set(lanes, cells, threads)
-    assert rle.tuning_get() == (lanes, cells, threads)
+    rle.tuning_set(lanes, cells, threads, staging)
+    assert rle.tuning_get() == (lanes, cells, threads, staging)
     try:
         for si, (scene, oscene) in enumerate(scenes):
             t0, s0 = oscene.levels[0][3], oscene.levels[0][4]
@@ -42,17 +42,18 @@ def test_shapes_bit_exact(rle, po, scenes, torch_cuda, shape, threads):
                 gpu = Frame(torch_cuda, rle, scene, rm).rays_host()
                 om = po.raymap_from_product(rm)
                 orc = po.render_rays(om, oscene, want_hits=True, want_counters=True)
-                assert_rays_equal(gpu, orc, f"scene {si} shape {shape} threads {threads} yaw {yaw}")
+                assert_rays_equal(gpu, orc, f"scene {si} shape {shape} threads {threads} staging {staging} yaw {yaw}")
                 assert counters_dict(gpu[3]) == oracle_counters(orc[3])
                 # without counters/hits the fast path (cells that may draw only)
                 fast = Frame(torch_cuda, rle, scene, rm, hits=False, counters=False).rays_host()
                 assert np.array_equal(fast[0], gpu[0]) and np.array_equal(fast[1].view(np.uint32),
                                                                           gpu[1].view(np.uint32))
     finally:
-        rle.tuning_set(0, 0, 0)
+        rle.tuning_set(0, 0, 0, 0)
 
 
 def test_tuning_rejects_bad_shapes(rle):
-    for lanes, cells, threads in ((3, 1, 128), (8, 1, 40), (8, 1, 256), (64, 1, 128), (32, 2, 128), (4, 1, 128)):
+    for lanes, cells, threads, staging in ((3, 1, 128, 0), (8, 1, 40, 0), (8, 1, 256, 0), (64, 1, 128, 0),
+                                           (32, 2, 128, 0), (4, 1, 128, 0), (32, 1, 128, 4), (32, 1, 128, -1)):
         with pytest.raises(rle.RLEError):
-            rle.tuning_set(lanes, cells, threads)
+            rle.tuning_set(lanes, cells, threads, staging)

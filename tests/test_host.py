@@ -141,7 +141,9 @@ def test_invalid_arguments_return_status(rle):
         rle.tuning_set(lanes_per_ray=12)
     with pytest.raises(rle.RLEError):
         rle.tuning_set(threads_per_block=48)
-    assert rle.tuning_get() == (0, 0, 0)
+    with pytest.raises(rle.RLEError):
+        rle.tuning_set(staging=4)
+    assert rle.tuning_get() == (0, 0, 0, 0)
 
 
 def test_malformed_rle4_rejected_before_upload(rle, po):
