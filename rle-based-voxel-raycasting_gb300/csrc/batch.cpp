@@ -103,7 +103,7 @@ void release(rle_batch* b) {
 
 rle_status prepare_grid(rle_batch* b) {
     rle_status st = rle::batch_grid_blocks(b->tuning.lanes_per_ray, b->tuning.threads_per_block, b->max_samples,
-                                           b->with_hits, &b->raycast_blocks);
+                                           b->with_hits, b->tuning.staging, &b->raycast_blocks);
     if (st != RLE_OK) return st;
     int sms = 0;
     const cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);

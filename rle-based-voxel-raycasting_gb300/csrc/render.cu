@@ -107,8 +107,10 @@ __device__ __forceinline__ uint32_t sm_id() {
     return s;
 }
 
-// Run-header staging (the launch's staging depth): 2 stages a cell's header
-// line in L2, 3 in L1, ahead of the scan that reads it.
+// Run-header staging (staging depth 2 or 3; the variants built with kStage):
+// 2 stages a cell's header line in L2, 3 in L1, ahead of the scan that reads
+// it.  Depth 1 variants carry none of this code: a runtime test in the chunk
+// loop measured 1% slower single frames and 4% slower batches at depth 1.
 __device__ __forceinline__ void stage_headers(const uint16_t* h, int staging) {
     if (staging == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(h));
     else if (staging >= 3) asm volatile("prefetch.global.L1 [%0];" ::"l"(h));
@@ -480,6 +482,21 @@ __device__ __forceinline__ void dda_step(Dda& d) {
     d.i0y = c1 ? d.i0y : a0y;
 }
 
+// The update half of dda_step (c1: the step's compare): the state after the
+// step.  The step's own values (dd_now, pnx, pny, index) are selects on the
+// state before it, which dda_chunk forms only where a lane captures them.
+__device__ __forceinline__ void dda_advance(Dda& d, bool c1) {
+    const float n1 = d.dd1 + d.gd1, n0 = d.dd0 + d.gd0;
+    const float a1x = d.i1x + d.g1x, a1y = d.i1y + d.g1y;
+    const float a0x = d.i0x + d.g0x, a0y = d.i0y + d.g0y;
+    d.dd1 = c1 ? n1 : d.dd1;
+    d.i1x = c1 ? a1x : d.i1x;
+    d.i1y = c1 ? a1y : d.i1y;
+    d.dd0 = c1 ? d.dd0 : n0;
+    d.i0x = c1 ? d.i0x : a0x;
+    d.i0y = c1 ? d.i0y : a0y;
+}
+
 // Level-of-detail switch at the top of a step (:343-365): past the switch
 // distance the ray moves to the next mip level and doubles its step.
 __device__ __forceinline__ void lod_switch(Walk& w, int nummaps) {
@@ -672,18 +689,19 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
     const int total = __shfl_sync(gmask, incl, lb + q.n - 1);
     for (int b = 0; b < total; b += G) {
         const int t = b + k;
-        // span of sample t: the first entry whose inclusive count exceeds t
-        int lo = 0, hi = q.n - 1;
-#pragma unroll
-        for (int it = 0; (1 << it) < G; it++) {
-            const int mid = (lo + hi) >> 1;
-            const int v = __shfl_sync(gmask, incl, lb + mid);
-            if (lo < hi) {
-                if (v > t) hi = mid;
-                else lo = mid + 1;
-            }
-        }
-        const int before = __shfl_sync(gmask, incl - cnt, lb + lo);
+        // span of sample t: entries start at strictly increasing sample
+        // numbers (every queued span owns at least one sample); those that
+        // start at or before b, plus those starting in (b, b + k], count
+        // the spans at or before t
+        const int start = incl - cnt;
+        const bool entry = k < q.n;
+        unsigned le = __ballot_sync(gmask, entry && start <= b) >> lb;
+        if constexpr (G < 32) le &= (1u << G) - 1u;
+        const unsigned marks =
+            __reduce_or_sync(gmask, (entry && start > b && start < b + G) ? (1u << (start - b)) : 0u);
+        const unsigned upto = k >= 31 ? 0xffffffffu : ((2u << k) - 1u);
+        const int lo = __popc(le) - 1 + __popc(marks & upto);
+        const int before = __shfl_sync(gmask, start, lb + lo);
         if (t < total) {
             const float4 e0 = q.e[kQueueVecs * lo], e1 = q.e[kQueueVecs * lo + 1], e2 = q.e[kQueueVecs * lo + 2];
             const uint32_t own0 = __float_as_uint(e0.y), own1 = __float_as_uint(e0.z);
@@ -729,18 +747,20 @@ __device__ __forceinline__ void flush_spans(const RayParams& P, SpanQueue& q, un
     q.n = 0;
 }
 
-// The exact walk over the runs prepare_cell recorded for one cell (same
-// tests, same order, same horizon updates as merge_cell).
+// The exact walk over the runs scan_runs recorded for one cell (same tests,
+// same order, same horizon updates as merge_cell).  a0: the first record when
+// the caller loaded it already (G < 32).
 template <int G, bool kDefer>
 __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& mask, unsigned gmask, int k,
-                                               uint32_t* row, float* drow, rle_hit* hrow, const float4* rec, int nrec,
+                                               uint32_t* row, float* drow, rle_hit* hrow, const float4* rec, float4 a0,
+                                               int nrec,
                                                float pz, float py, int mip, int vx, int vz, int& ymin, int& ymax,
                                                Pending& pend, SpanQueue& q, Counts& cnt) {
     const float res_y2 = static_cast<float>(P.S / 2);
     // clip top (:467)
     if (pz * res_y2 + py <= pz * static_cast<float>(ymin)) return;
     for (int r = 0; r < nrec; r++) {
-        const float4 a = rec[3 * r];
+        const float4 a = (G < 32 && r == 0) ? a0 : rec[3 * r];
         if (__float_as_int(a.x) <= ymin) break;
         int scr_y2 = __float_as_int(a.y), scr_y1 = __float_as_int(a.z);
         if (scr_y1 >= ymax) continue;
@@ -775,8 +795,11 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
             const uint32_t r1 = hi_bits > 0 ? ((1u << hi_bits) - 1u) : 0u;
             const uint32_t m0 = mask.w[wi], m1 = r1 ? mask.w[wi + 1] : 0u;
             const uint32_t own0 = r0 & ~m0, own1 = r1 & ~m1;
-            __syncwarp(gmask);
-            if (k == 0) {
+            __syncwarp(gmask);  // every lane has read m0, m1 before any lane stores
+            {
+                // Every lane stores the same words (the merge is uniform over the
+                // group), so each lane later reads back its own stores: no branch
+                // to one lane and no second barrier.
                 mask.w[wi] = m0 | r0;
                 if (r1) mask.w[wi + 1] = m1 | r1;
                 float4* e = q.e + kQueueVecs * q.n;
@@ -788,7 +811,6 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
                                                         (static_cast<uint32_t>(colours_in_run) << 16)),
                                    d.w, __uint_as_float(static_cast<uint32_t>(vx) | (static_cast<uint32_t>(vz) << 16)));
             }
-            __syncwarp(gmask);
             q.n++;
             continue;
         }
@@ -830,12 +852,23 @@ __device__ __forceinline__ int dda_chunk(const RayParams& P, Walk& W, int k, uns
     if (plain) {
 #pragma unroll
         for (int s = 0; s < G; s++) {
-            dda_step(W.d);
-            if (s == k) {
-                c_dd = W.d.dd_now;
-                c_px = W.d.pnx;
-                c_py = W.d.pny;
-                c_ix = W.d.index;
+            if (s == G - 1) {
+                dda_step(W.d);
+                if (s == k) {
+                    c_dd = W.d.dd_now;
+                    c_px = W.d.pnx;
+                    c_py = W.d.pny;
+                    c_ix = W.d.index;
+                }
+            } else {
+                const bool c1 = W.d.dd1 < W.d.dd0;
+                if (s == k) {
+                    c_dd = c1 ? W.d.dd1 : W.d.dd0;
+                    c_px = c1 ? W.d.i1x : W.d.i0x;
+                    c_py = c1 ? W.d.i1y : W.d.i0y;
+                    c_ix = c1 ? 1 : 0;
+                }
+                dda_advance(W.d, c1);
             }
         }
         W.z += W.dz * static_cast<float>(G);
@@ -916,7 +949,7 @@ __device__ __forceinline__ bool ray_is_done(const RayParams& P, const Ray& R, fl
 // gmask), using mask_words (S/32 words of shared memory) as its bitmask.
 // active = false: the lanes only take part in the group's collectives.
 // chunks of G DDA steps, lane k taking step k of each.
-template <int G, bool kCount, bool kHits, bool kDefer>
+template <int G, bool kCount, bool kHits, bool kDefer, bool kStage>
 __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active, uint32_t* mask_words, float4* recs,
                                          float4* spans, int k, unsigned gmask, int staging, Counts& cnt) {
     const int S = P.S;
@@ -1001,6 +1034,12 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                 const int s = __ffs(todo) - 1;
                 todo &= todo - 1;
                 const int src = lane_base(gmask) + s;
+                const float4* rec = recs + static_cast<size_t>((threadIdx.x & ~31u) + src) * (3 * kRecs);
+                // with several rays per warp, the cell's first record is loaded
+                // beside the shuffles that fetch its values (measured: batches
+                // -4%; single frames at 32 lanes +1.6%, so not there)
+                float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (G < 32) a0 = rec[0];
                 const float pz = __shfl_sync(gmask, c.pz, src);
                 const float py = __shfl_sync(gmask, c.py, src);
                 const int packed = __shfl_sync(gmask, (c.nrec + 1) | (c.mip << 8), src);
@@ -1031,10 +1070,9 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
                     cs.loaded = __shfl_sync(gmask, static_cast<int>(c.loaded), src) != 0;
                     merge_cell<G, kCount>(P, R, mask, gmask, k, row, drow, hrow, cs, ymin, ymax, pend, cnt);
                 } else {
-                    const float4* rec = recs + static_cast<size_t>((threadIdx.x & ~31u) + src) * (3 * kRecs);
                     const int ymin_before = ymin;
-                    merge_recorded<G, kDefer>(P, mask, gmask, k, row, drow, hrow, rec, nrec, pz, py, mip, vx, vz, ymin,
-                                              ymax, pend, q, cnt);
+                    merge_recorded<G, kDefer>(P, mask, gmask, k, row, drow, hrow, rec, a0, nrec, pz, py, mip, vx, vz,
+                                              ymin, ymax, pend, q, cnt);
                     if (ymin != ymin_before) {
                         // cells whose first recorded run now breaks the walk
                         // at once are no-ops: drop them all in one vote
@@ -1055,7 +1093,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
             // under the merge; stage each cell's header line (second header
             // on; the first travels in the table entry) for its scan, which
             // follows the next DDA chunk
-            if (staging >= 2 && c_next.loaded && (c_next.ey & 0xffffu) > 1u)
+            if (kStage && c_next.loaded && (c_next.ey & 0xffffu) > 1u)
                 stage_headers(P.slabs[c_next.mip] + 3 + c_next.ex, staging);
             c = c_next;
             nvalid = nvalid_next;
@@ -1118,8 +1156,9 @@ struct Lanes {
 };
 
 // One frame: ray slot s of block b casts ray b * slots + s.  kCount: the
-// DETAIL_BENCH counters (exact walk of every cell); kHits: hit records.
-template <int G, bool kCount, bool kHits, bool kDefer>
+// DETAIL_BENCH counters (exact walk of every cell); kHits: hit records;
+// kDefer: packed fill of short spans; kStage: run-header staging (depth 2/3).
+template <int G, bool kCount, bool kHits, bool kDefer, bool kStage>
 __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ RayParams P) {
     extern __shared__ uint32_t smem[];
     const Lanes<G> L;
@@ -1138,8 +1177,8 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
         t->start_ns = global_ns();
         t->start_clock = static_cast<uint64_t>(clock64());
     }
-    cast_ray<G, kCount, kHits, kDefer>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask, P.staging,
-                                       cnt);
+    cast_ray<G, kCount, kHits, kDefer, kStage>(P, x, x < P.rays, smem + L.slot * words, recs, spans, L.k, L.gmask,
+                                               P.staging, cnt);
     if (P.ray_time && L.k == 0 && x < P.rays) {
         rle_ray_time* t = P.ray_time + x;
         t->end_clock = static_cast<uint64_t>(clock64());
@@ -1153,7 +1192,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const __grid_constant__ Ra
 // index space (ray_start[f] = first global ray of frame f); each group takes
 // `tile` consecutive rays at a time from a global counter until none are
 // left, so long and short rays of every frame balance across the GPU.
-template <int G, bool kHits, bool kDefer>
+template <int G, bool kHits, bool kDefer, bool kStage>
 __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, const int* __restrict__ ray_start,
                                                             const RayParams* __restrict__ frames, int tile,
                                                             int staging, int max_words) {
@@ -1195,13 +1234,13 @@ __global__ void __launch_bounds__(128) raycast_batch_kernel(BatchHeader* hdr, co
                 }
                 f = lo;
             }
-            cast_ray<G, false, kHits, kDefer>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k, L.gmask,
-                                             staging, cnt);
+            cast_ray<G, false, kHits, kDefer, kStage>(frames[f], r - ray_start[f], true, mask_words, recs, spans, L.k,
+                                                     L.gmask, staging, cnt);
         }
     }
 }
 
-template <int G, bool kCount, bool kHits, bool kDefer>
+template <int G, bool kCount, bool kHits, bool kDefer, bool kStage>
 rle_status launch_variant(const RayParams& p, int threads, cudaStream_t stream) {
     const int words = (p.S + 31) >> 5;
     const int rays_per_block = threads / 32 * (32 / G);
@@ -1210,14 +1249,14 @@ rle_status launch_variant(const RayParams& p, int threads, cudaStream_t stream) 
         set_error("rle_render_rays: %d samples per ray exceed shared memory at this launch shape", p.S);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<G, kCount, kHits, kDefer>,
+    cudaError_t e = cudaFuncSetAttribute(raycast_kernel<G, kCount, kHits, kDefer, kStage>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) {
         set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
     }
     const int blocks = (p.rays + rays_per_block - 1) / rays_per_block;
-    raycast_kernel<G, kCount, kHits, kDefer><<<blocks, threads, smem, stream>>>(p);
+    raycast_kernel<G, kCount, kHits, kDefer, kStage><<<blocks, threads, smem, stream>>>(p);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("raycast launch: %s", cudaGetErrorString(e));
@@ -1226,18 +1265,23 @@ rle_status launch_variant(const RayParams& p, int threads, cudaStream_t stream) 
     return RLE_OK;
 }
 
+template <int G, bool kStage>
+rle_status launch_output(const RayParams& p, int threads, cudaStream_t stream) {
+    if (p.S <= kDeferMaxSamples) {
+        return p.rayhit ? launch_variant<G, false, true, true, kStage>(p, threads, stream)
+                        : launch_variant<G, false, false, true, kStage>(p, threads, stream);
+    }
+    return p.rayhit ? launch_variant<G, false, true, false, kStage>(p, threads, stream)
+                    : launch_variant<G, false, false, false, kStage>(p, threads, stream);
+}
+
 template <int G>
 rle_status launch_shape(const RayParams& p, int threads, cudaStream_t stream) {
-    if (p.counters) {
-        return p.rayhit ? launch_variant<G, true, true, false>(p, threads, stream)
-                        : launch_variant<G, true, false, false>(p, threads, stream);
+    if (p.counters) {  // the counts do not depend on the staging depth
+        return p.rayhit ? launch_variant<G, true, true, false, false>(p, threads, stream)
+                        : launch_variant<G, true, false, false, false>(p, threads, stream);
     }
-    if (p.S <= kDeferMaxSamples) {
-        return p.rayhit ? launch_variant<G, false, true, true>(p, threads, stream)
-                        : launch_variant<G, false, false, true>(p, threads, stream);
-    }
-    return p.rayhit ? launch_variant<G, false, true, false>(p, threads, stream)
-                    : launch_variant<G, false, false, false>(p, threads, stream);
+    return p.staging >= 2 ? launch_output<G, true>(p, threads, stream) : launch_output<G, false>(p, threads, stream);
 }
 
 template <int G, bool kDefer>
@@ -1245,21 +1289,21 @@ size_t batch_smem(int threads, int max_samples) {
     return raycast_smem_bytes(threads, threads / 32 * (32 / G), (max_samples + 31) >> 5, kDefer);
 }
 
-template <int G, bool kHits, bool kDefer>
+template <int G, bool kHits, bool kDefer, bool kStage>
 rle_status batch_blocks(int threads, int max_samples, int* blocks) {
     const size_t smem = batch_smem<G, kDefer>(threads, max_samples);
     if (smem > 227 * 1024) {
         set_error("batch: %d samples per ray exceed shared memory at this launch shape", max_samples);
         return RLE_ERR_CAPACITY;
     }
-    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G, kHits, kDefer>,
+    cudaError_t e = cudaFuncSetAttribute(raycast_batch_kernel<G, kHits, kDefer, kStage>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int dev = 0, sms = 0, per_sm = 0;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G, kHits, kDefer>, threads,
-                                                          smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raycast_batch_kernel<G, kHits, kDefer, kStage>,
+                                                          threads, smem);
     if (e != cudaSuccess) {
         set_error("batch launch set-up: %s", cudaGetErrorString(e));
         return RLE_ERR_CUDA;
@@ -1268,15 +1312,15 @@ rle_status batch_blocks(int threads, int max_samples, int* blocks) {
     return RLE_OK;
 }
 
-template <int G, bool kHits, bool kDefer>
+template <int G, bool kHits, bool kDefer, bool kStage>
 rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
     const size_t smem = batch_smem<G, kDefer>(b.threads, b.max_samples);
     int blocks = b.blocks;
     if (blocks <= 0) {
-        const rle_status st = batch_blocks<G, kHits, kDefer>(b.threads, b.max_samples, &blocks);
+        const rle_status st = batch_blocks<G, kHits, kDefer, kStage>(b.threads, b.max_samples, &blocks);
         if (st != RLE_OK) return st;
     }
-    raycast_batch_kernel<G, kHits, kDefer><<<blocks, b.threads, smem, stream>>>(
+    raycast_batch_kernel<G, kHits, kDefer, kStage><<<blocks, b.threads, smem, stream>>>(
         b.header, b.ray_start, b.frames, b.tile, b.staging, (b.max_samples + 31) >> 5);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -1287,27 +1331,33 @@ rle_status batch_launch(const BatchRaycast& b, cudaStream_t stream) {
 }
 
 template <int G, bool kDefer>
-rle_status batch_blocks_for(int threads, int max_samples, bool hits, int* blocks) {
-    return hits ? batch_blocks<G, true, kDefer>(threads, max_samples, blocks)
-                : batch_blocks<G, false, kDefer>(threads, max_samples, blocks);
+rle_status batch_blocks_for(int threads, int max_samples, bool hits, bool stage, int* blocks) {
+    if (stage)
+        return hits ? batch_blocks<G, true, kDefer, true>(threads, max_samples, blocks)
+                    : batch_blocks<G, false, kDefer, true>(threads, max_samples, blocks);
+    return hits ? batch_blocks<G, true, kDefer, false>(threads, max_samples, blocks)
+                : batch_blocks<G, false, kDefer, false>(threads, max_samples, blocks);
 }
 
 template <int G, bool kDefer>
 rle_status batch_launch_for(const BatchRaycast& b, cudaStream_t s) {
-    return b.hits ? batch_launch<G, true, kDefer>(b, s) : batch_launch<G, false, kDefer>(b, s);
+    if (b.staging >= 2)
+        return b.hits ? batch_launch<G, true, kDefer, true>(b, s) : batch_launch<G, false, kDefer, true>(b, s);
+    return b.hits ? batch_launch<G, true, kDefer, false>(b, s) : batch_launch<G, false, kDefer, false>(b, s);
 }
 
 }  // namespace
 
-rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks) {
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int staging, int* blocks) {
     const bool defer = max_samples <= kDeferMaxSamples;
+    const bool stage = staging >= 2;
     switch (lanes) {
-        case 8: return defer ? batch_blocks_for<8, true>(threads, max_samples, hits, blocks)
-                             : batch_blocks_for<8, false>(threads, max_samples, hits, blocks);
-        case 16: return defer ? batch_blocks_for<16, true>(threads, max_samples, hits, blocks)
-                              : batch_blocks_for<16, false>(threads, max_samples, hits, blocks);
-        case 32: return defer ? batch_blocks_for<32, true>(threads, max_samples, hits, blocks)
-                              : batch_blocks_for<32, false>(threads, max_samples, hits, blocks);
+        case 8: return defer ? batch_blocks_for<8, true>(threads, max_samples, hits, stage, blocks)
+                             : batch_blocks_for<8, false>(threads, max_samples, hits, stage, blocks);
+        case 16: return defer ? batch_blocks_for<16, true>(threads, max_samples, hits, stage, blocks)
+                              : batch_blocks_for<16, false>(threads, max_samples, hits, stage, blocks);
+        case 32: return defer ? batch_blocks_for<32, true>(threads, max_samples, hits, stage, blocks)
+                              : batch_blocks_for<32, false>(threads, max_samples, hits, stage, blocks);
         default:
             set_error("batch: lanes per ray must be 8, 16 or 32");
             return RLE_ERR_INVALID_ARG;

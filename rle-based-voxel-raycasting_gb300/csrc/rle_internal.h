@@ -170,7 +170,7 @@ rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, con
                                void* stream);
 size_t batch_capacity_words(const rle_batch* b);
 int batch_max_frames(const rle_batch* b);
-rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int* blocks);
+rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int staging, int* blocks);
 
 // Bounds-check words of the device code (zeros when none fired); false in
 // builds without RLE_BOUNDS_CHECK.  read: flags, first index hit; clear
