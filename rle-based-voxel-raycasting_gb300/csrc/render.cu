@@ -969,7 +969,10 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
         R.ymin = 0;
         R.ymax = -1;
     }
-    __syncwarp();
+    // the group's lanes order among themselves only: with several rays per
+    // warp the other group may be at another ray (the persistent batch
+    // launch claims rays per group)
+    __syncwarp(gmask);
     uint32_t* row = active ? P.raybuf + static_cast<size_t>(x) * S : nullptr;
     float* drow = active ? P.raydepth + static_cast<size_t>(x) * S : nullptr;
     rle_hit* hrow = nullptr;
@@ -1101,7 +1104,7 @@ __device__ __forceinline__ void cast_ray(const RayParams& P, int x, bool active,
     }
     flush_spans<G>(P, q, gmask, k, row, drow, hrow, pend);
     pend.flush();
-    __syncwarp();
+    __syncwarp(gmask);
 
     // ---- coalesced fill of the samples no span coloured ----
     if (active) {
