@@ -71,6 +71,22 @@ E2E_FRAMES_IN_FLIGHT = 6
 E2E_LANES_PER_RAY = 16
 
 
+def bench_config(rays_per_frame, runs_per_column: float, world: int) -> dict:
+    """The workload description both arms print (the GPU arm and
+    `--impl reference`), key for key and value for value, so that their lines
+    describe the same run: the same frames of the same scene, their mean
+    column rays, the scene's runs per column, and how each arm treats the
+    L2 and the ranks."""
+    return {
+        "workload": WORKLOAD,
+        "samples_per_ray": pow2_ceil(W),
+        "column_rays_per_frame": round(sum(rays_per_frame) / len(rays_per_frame), 1),
+        "runs_per_column": round(runs_per_column, 2),
+        "l2": "GPU arm: flushed before every step (256 MiB write); the host arm has no GPU cache to flush",
+        "parallelism": f"replicas x{world}: every rank renders its own camera path; the host arm runs on rank 0's cores",
+    }
+
+
 def pow2_ceil(v: int) -> int:
     p = 1
     while p < v:
@@ -428,15 +444,8 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded scene and camera path)",
-        "config": {
-            "workload": WORKLOAD,
-            "scene_device_bytes": int(info.device_bytes),
-            "runs_per_column": round(info.run_headers / (SCENE["n"] ** 2), 2),
-            "column_rays_per_frame": round(sum(rays) / len(rays), 1),
-            "samples_per_ray": rms[0].samples,
-            "l2": "flushed between steps (256 MiB write)",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": bench_config(rays, info.run_headers / (SCENE["n"] ** 2), world),
+        "scene": {"device_bytes": int(info.device_bytes)},
         "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 28,
                 "d2h_bytes_per_step": W * H * 8,
                 "pipeline": f"multi-buffered frame loop: frames rotate over {E2E_FRAMES_IN_FLIGHT} streams; a frame's read-back and last rays overlap the next frames' renders",
@@ -877,6 +886,7 @@ def run_reference(args):
     po.build_oracle()
     oscene = po.OracleScene.from_rle4(data)
     sx, sy, sz, table, words = oscene.levels[0]
+    run_headers = int((table[1::2] & 0xFFFF).astype(np.int64).sum())
     cams = poses(rle, (sx, sy, sz, table, words), args.warmup + args.steps)
     threads = os.cpu_count() or 1
 
@@ -900,13 +910,11 @@ def run_reference(args):
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and camera path)",
-        "config": {"workload": WORKLOAD, "samples_per_ray": pow2_ceil(W),
-                   "column_rays_per_frame": round(sum(rays) / len(rays), 1),
-                   "parallelism": f"host: OpenMP over column rays, {threads} threads"},
+        "config": bench_config(rays, run_headers / (SCENE["n"] ** 2), world),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} frame(s): ray map + Render::render_line port + resolve, "
-                                   f"OpenMP over column rays"},
+                                   f"OpenMP over column rays, {threads} threads"},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

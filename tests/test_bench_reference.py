@@ -26,6 +26,10 @@ def test_reference_arm_json_line():
     assert line["unit"] == "Mrays/s" and line["higher_is_better"] is True and line["value"] > 0
     assert line["config"]["workload"].startswith("config 2: 2048x2048x256")
     assert line["config"]["samples_per_ray"] == 2048
+    # the GPU arm prints the same workload description (bench.bench_config), key for key
+    assert set(line["config"]) == {"workload", "samples_per_ray", "column_rays_per_frame", "runs_per_column", "l2",
+                                   "parallelism"}
+    assert 5.0 < line["config"]["runs_per_column"] < 12.0 and line["config"]["column_rays_per_frame"] > 1000
     cb = line["cpu_baseline"]
     assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     e2e = line["e2e"]
