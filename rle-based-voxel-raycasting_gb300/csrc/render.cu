@@ -774,12 +774,16 @@ __device__ __forceinline__ void merge_recorded(const RayParams& P, const Mask& m
             scr_y2 = ymax;
             ymax = scr_y1;
         }
+        // the first free sample of the span: a span reaching ymin starts there,
+        // since ymin always names a free sample (or the range is closed, and
+        // then y >= scr_y2 as in the walk), so only the other spans scan the mask
+        int y;
         if (scr_y1 <= ymin) {
-            scr_y1 = ymin;
-            ymin = scr_y2;
-            ymin = mask.first_clear(ymin, ymax > ymin ? ymax : ymin);
+            y = ymin;
+            ymin = mask.first_clear(scr_y2, ymax > scr_y2 ? ymax : scr_y2);
+        } else {
+            y = mask.first_clear(scr_y1, scr_y2);
         }
-        const int y = mask.first_clear(scr_y1, scr_y2);
         if (y >= scr_y2) continue;
         const float4 b = rec[3 * r + 1], d = rec[3 * r + 2];
         Span sp;
