@@ -155,18 +155,20 @@ RLE_HD int tint(const Consts& p, int x, int z) {
 // RGB565 colour of level-0 voxel (x, j, z), j counted down from the top,
 // given the column's tint: a height-band palette scaled by tint + jitter.
 RLE_HD uint16_t colour(const Consts& p, int tint_xz, int x, int j, int z) {
-    // palette bands, bottom to top: 0xRRGGBB
-    const uint32_t kPal[8] = {0x5C4E42u, 0x96825Au, 0xC4B478u, 0x609646u,
-                              0x467C3Au, 0x767064u, 0x96928Cu, 0xECECF0u};
+    // palette bands, bottom to top: 0x5C4E42, 0x96825A, 0xC4B478, 0x609646,
+    // 0x467C3A, 0x767064, 0x96928C, 0xECECF0 (0xRRGGBB), held as one byte per
+    // band in each channel's constant (band b in bits 8b..8b+7), so that no
+    // thread builds a table in local memory
+    const uint64_t kPalR = 0xEC96764660C4965Cull, kPalG = 0xEC92707C96B4824Eull, kPalB = 0xF08C643A46785A42ull;
     const int y = p.sy - 1 - j;
     int band = y * 8 / p.sy;
     if (band > 7) band = 7;
     if (band < 0) band = 0;
     const int jitter = static_cast<int>(hash32(x, y, z, p.seed32) & 31);
     const int f = 176 + tint_xz + jitter;  // 176..303, /256
-    const uint32_t c = kPal[band];
-    int r = static_cast<int>(c >> 16) * f >> 8, g = static_cast<int>((c >> 8) & 255) * f >> 8,
-        b = static_cast<int>(c & 255) * f >> 8;
+    const int sh = 8 * band;
+    int r = static_cast<int>((kPalR >> sh) & 255u) * f >> 8, g = static_cast<int>((kPalG >> sh) & 255u) * f >> 8,
+        b = static_cast<int>((kPalB >> sh) & 255u) * f >> 8;
     if (r > 255) r = 255;
     if (g > 255) g = 255;
     if (b > 255) b = 255;
