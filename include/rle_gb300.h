@@ -329,13 +329,19 @@ rle_status rle_render_frame(const rle_scene* scene, const rle_camera* cam,
 /* Batched rendering                                                      */
 /* ---------------------------------------------------------------------- */
 
-/* Many cameras -- any mix of resolutions -- rendered by one persistent
- * raycast launch and one resolve launch: the column rays of all frames form
- * one work queue that lane groups drain tile by tile, so short and long rays
- * of every frame balance across the GPU.  The two launches (and the upload
- * of the per-frame parameters) are captured once into a CUDA graph and
- * replayed for every batch.  No counterpart in the reference, which renders
- * one camera per launch (src/Cuda_Main.cu:183-271). */
+/* Many cameras -- any mix of resolutions -- in one call, in one of two
+ * launch modes (rle_batch_tuning.per_frame):
+ *   per-frame (default): one raycast + resolve launch pair per frame, the
+ *     frames forked over eight worker streams of the batch and joined back
+ *     on the caller's stream, so up to eight frames are in flight and one
+ *     frame's slowest column rays overlap the next frames';
+ *   persistent: one raycast launch and one resolve launch for the whole
+ *     batch -- the column rays of all frames form one work queue that lane
+ *     groups drain tile by tile -- captured once (with the upload of the
+ *     per-frame parameters) into a CUDA graph and replayed for every batch.
+ * rle_batch_autotune times both over its launch shapes.  No counterpart in
+ * the reference, which renders one camera per launch
+ * (src/Cuda_Main.cu:183-271). */
 typedef struct rle_batch rle_batch;
 
 typedef struct rle_frame_request {
@@ -353,8 +359,10 @@ typedef struct rle_batch_tuning {
     int staging;            /* staging depth of the column data, 1..3, as rle_tuning.staging */
     int threads_per_block;  /* 32, 64, 96 or 128 */
     int use_graph;          /* 1: capture once and replay (default); 0: plain launches */
-    int per_frame;          /* 1: one plain raycast + resolve launch per frame instead of the
-                               persistent pair (wins for a few large frames); 0 default */
+    int per_frame;          /* 1 (default): one plain raycast + resolve launch pair per frame,
+                               the frames forked over eight worker streams of the batch (up
+                               to eight in flight) and joined back on the caller's stream;
+                               0: the persistent pair */
 } rle_batch_tuning;
 
 /* max_frames per batch; raybuf_words: ray-buffer capacity shared by the
@@ -402,6 +410,8 @@ typedef struct rle_server_config {
     size_t raybuf_words;          /* ray-buffer words of each batch slot */
     int max_samples;              /* widest samples-per-ray accepted */
     int plain;                    /* 1: one request per launch, one at a time (for comparison) */
+    rle_batch_tuning batch_tuning; /* launch shape of the batch slots (rle_batch_set_tuning);
+                                      all zero: the batch default (per-frame, 32 lanes) */
 } rle_server_config;
 
 typedef struct rle_request {

@@ -104,7 +104,8 @@ class BatchTuning(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("hbm_budget_bytes", C.c_size_t), ("max_frames_per_batch", C.c_int),
-                ("max_inflight", C.c_int), ("raybuf_words", C.c_size_t), ("max_samples", C.c_int), ("plain", C.c_int)]
+                ("max_inflight", C.c_int), ("raybuf_words", C.c_size_t), ("max_samples", C.c_int), ("plain", C.c_int),
+                ("batch_tuning", BatchTuning)]
 
 
 class Request(C.Structure):
@@ -494,9 +495,10 @@ class Server:
     launch per request)."""
 
     def __init__(self, hbm_budget_bytes: int, raybuf_words: int, max_frames_per_batch: int = 64,
-                 max_inflight: int = 2, max_samples: int = 1920, plain: bool = False, device: int = 0):
+                 max_inflight: int = 2, max_samples: int = 1920, plain: bool = False, device: int = 0,
+                 batch_tuning: Optional[BatchTuning] = None):
         cfg = ServerConfig(device, hbm_budget_bytes, max_frames_per_batch, max_inflight, raybuf_words, max_samples,
-                           int(plain))
+                           int(plain), batch_tuning if batch_tuning is not None else BatchTuning())
         h = C.c_void_p()
         _check(_lib.rle_server_create(C.byref(cfg), C.byref(h)), "rle_server_create")
         self._h = h

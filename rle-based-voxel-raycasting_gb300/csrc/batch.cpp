@@ -1,5 +1,7 @@
-// Batched rendering: many cameras in one persistent raycast launch and one
-// persistent resolve launch, captured once into a CUDA graph.
+// Batched rendering: many cameras per call, either as one plain launch pair
+// per frame forked over worker streams (the default) or as one persistent
+// raycast launch and one persistent resolve launch, captured once into a
+// CUDA graph.
 //
 // Per batch the host builds every frame's ray map, packs the per-frame
 // kernel parameters, the ray and pixel-block prefix sums and the frame count
@@ -64,7 +66,16 @@ struct rle_batch {
     int parity = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    rle_batch_tuning tuning{1, 32, 1, 128, 1, 0};
+    // per-frame mode: the frames' launch pairs fork over these streams and
+    // join back on the caller's stream
+    static constexpr int kWorkers = 8;
+    cudaStream_t workers[kWorkers] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t joins[kWorkers] = {};
+    // per-frame launches at 32 lanes: measured ahead of the persistent pair
+    // on batches of 1080p frames, on the config-3 mix and in the config-4
+    // server (lower latency and higher saturated throughput)
+    rle_batch_tuning tuning{1, 32, 1, 128, 1, 1};
     int raycast_blocks = 0;
     int resolve_blocks = 0;
     std::mutex mu;
@@ -93,6 +104,14 @@ void release(rle_batch* b) {
         if (b->h_params[i]) cudaFreeHost(b->h_params[i]);
     }
     if (b->capture) cudaStreamDestroy(b->capture);
+    for (int w = 0; w < rle_batch::kWorkers; w++) {
+        if (b->workers[w]) {
+            cudaStreamSynchronize(b->workers[w]);
+            cudaStreamDestroy(b->workers[w]);
+        }
+        if (b->joins[w]) cudaEventDestroy(b->joins[w]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->d_raybuf) cudaFree(b->d_raybuf);
     if (b->d_raydepth) cudaFree(b->d_raydepth);
     if (b->d_rayhit) cudaFree(b->d_rayhit);
@@ -228,16 +247,31 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
         if (st != RLE_OK) return st;
     }
     if (b->tuning.per_frame) {
-        // one plain launch pair per frame, parameters by value from the staging block
+        // one plain launch pair per frame, parameters by value from the
+        // staging block; frame i goes to worker stream i % k, so up to k
+        // frames are in flight and one frame's slowest rays overlap the next
+        // frames' (each frame has its own rows of the ray buffer); the
+        // workers fork from and join back onto the caller's stream
         const Layout& L = b->layout;
         auto* rp = reinterpret_cast<rle::RayParams*>(b->h_params[par] + L.ray_params);
         auto* sp = reinterpret_cast<rle::ResolveParams*>(b->h_params[par] + L.resolve_params);
+        const int k = std::min(n, rle_batch::kWorkers);
+        cudaError_t e = cudaEventRecord(b->fork, stream);
+        for (int w = 0; w < k && e == cudaSuccess; w++) e = cudaStreamWaitEvent(b->workers[w], b->fork, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "rle_batch_render: fork to the worker streams");
         for (int i = 0; i < n && st == RLE_OK; i++) {
             rp[i].lanes_per_ray = b->tuning.lanes_per_ray;
             rp[i].threads_per_block = b->tuning.threads_per_block;
             rp[i].staging = b->tuning.staging;
-            st = rle::launch_raycast(rp[i], stream);
-            if (st == RLE_OK) st = rle::launch_resolve(sp[i], stream);
+            st = rle::launch_raycast(rp[i], b->workers[i % k]);
+            if (st == RLE_OK) st = rle::launch_resolve(sp[i], b->workers[i % k]);
+        }
+        // joined even after a failed launch: the caller's stream never runs
+        // ahead of work already queued
+        for (int w = 0; w < k; w++) {
+            const cudaError_t ej = cudaEventRecord(b->joins[w], b->workers[w]);
+            const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(stream, b->joins[w], 0) : ej;
+            if (ew != cudaSuccess && st == RLE_OK) st = cuda_fail(ew, "rle_batch_render: join of the worker streams");
         }
         if (st != RLE_OK) return st;
     } else if (b->tuning.use_graph) {
@@ -326,6 +360,14 @@ extern "C" rle_status rle_batch_create(int device, int max_frames, size_t raybuf
     }
     if (st == RLE_OK && (e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking)) != cudaSuccess)
         st = cuda_fail(e, "cudaStreamCreate");
+    if (st == RLE_OK && (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess)
+        st = cuda_fail(e, "cudaEventCreate");
+    for (int w = 0; w < rle_batch::kWorkers && st == RLE_OK; w++) {
+        if ((e = cudaStreamCreateWithFlags(&b->workers[w], cudaStreamNonBlocking)) != cudaSuccess)
+            st = cuda_fail(e, "cudaStreamCreate");
+        else if ((e = cudaEventCreateWithFlags(&b->joins[w], cudaEventDisableTiming)) != cudaSuccess)
+            st = cuda_fail(e, "cudaEventCreate");
+    }
     if (st != RLE_OK) {
         release(b);
         return st;

@@ -308,6 +308,8 @@ extern "C" rle_status rle_server_create(const rle_server_config* cfg, rle_server
         } else {
             st = rle_batch_create(cfg->device, cfg->max_frames_per_batch, cfg->raybuf_words, cfg->max_samples, 0,
                                   &sl.batch);
+            if (st == RLE_OK && cfg->batch_tuning.lanes_per_ray != 0)
+                st = rle_batch_set_tuning(sl.batch, &cfg->batch_tuning);
         }
     }
     if (prev >= 0) cudaSetDevice(prev);

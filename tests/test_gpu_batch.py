@@ -251,8 +251,10 @@ def test_consecutive_batches_on_two_streams(rle, po, scene_pair, torch_cuda):
     b = rle.Batch(max_frames=8, raybuf_words=words, max_samples=1024)
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     torch.cuda.synchronize()
-    for use_graph in (1, 0):
-        b.set_tuning(1, 32, 1, 128, use_graph, 0)
+    # the persistent launches with and without the graph, and the per-frame
+    # launches forked over the batch's worker streams
+    for use_graph, per_frame in ((1, 0), (0, 0), (0, 1)):
+        b.set_tuning(1, 32 if not per_frame else 16, 1, 128, use_graph, per_frame)
         for _ in range(3):
             b.render(scene, outs_a.reqs, stream=s1.cuda_stream)
             b.render(scene, outs_b.reqs, stream=s2.cuda_stream)
@@ -260,5 +262,5 @@ def test_consecutive_batches_on_two_streams(rle, po, scene_pair, torch_cuda):
         for cams, outs, tag in ((cams_a, outs_a, "stream 1"), (cams_b, outs_b, "stream 2")):
             for i, (cam, view) in enumerate(cams):
                 assert_screen_equal(outs.host(rle, i), oracle_screen(po, rle, oscene, cam, view, hits=False),
-                                    f"{tag} graph={use_graph} frame {i}")
+                                    f"{tag} graph={use_graph} per_frame={per_frame} frame {i}")
     b.free()

@@ -70,12 +70,23 @@ def _alone(rle, torch, scene, cam, view):
     return c.cpu().numpy().view(np.uint32), d.cpu().numpy()
 
 
-@pytest.mark.parametrize("plain", [False, True])
-def test_served_results_equal_alone(rle, po, scene_pairs, torch_cuda, plain):
+# batched: the slots' default launch shape (per-frame launches over worker
+# streams); persistent: the slots' persistent pair; plain: one launch per request
+MODES = {"batched": None, "persistent": (1, 32, 1, 128, 1, 0), "plain": None}
+
+
+def _server(rle, mode, **kw):
+    tun = MODES[mode]
+    return rle.Server(plain=mode == "plain", batch_tuning=rle.BatchTuning(*tun) if tun else None, **kw)
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_served_results_equal_alone(rle, po, scene_pairs, torch_cuda, mode):
     torch = torch_cuda
+    plain = mode == "plain"
     scenes = [s for s, _ in scene_pairs]
-    srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
-                     max_samples=640, plain=plain)
+    srv = _server(rle, mode, hbm_budget_bytes=8 << 30, raybuf_words=8 << 20, max_frames_per_batch=8, max_inflight=3,
+                  max_samples=640)
     ids = [srv.add_scene(s) for s in scenes]
     assert ids == [0, 1]
     reqs = _requests(rle, scenes, 24, 7)
@@ -243,8 +254,8 @@ def _pow2_ceil(v):
     return p
 
 
-@pytest.mark.parametrize("plain", [False, True])
-def test_config4_mix_against_oracle(rle, po, torch_cuda, plain):
+@pytest.mark.parametrize("mode", list(MODES))
+def test_config4_mix_against_oracle(rle, po, torch_cuda, mode):
     """A config-4 served mix: two resident cave scenes of different sizes
     (1024^2 and 2048^2 x 256, seeds 3 and 4), 40 requests with the config's
     resolution law (256x256 .4, 640x480 .3, 1280x720 .2, 1920x1080 .1; every
@@ -256,8 +267,9 @@ def test_config4_mix_against_oracle(rle, po, torch_cuda, plain):
     for n, seed in ((1024, 3), (2048, 4)):
         data = rle.scenegen_rle4(rle.scenegen_default(n, 256, n, seed, caves=True))
         pairs.append((rle.Scene.from_bytes(data), po.OracleScene.from_rle4(data), n))
-    srv = rle.Server(hbm_budget_bytes=16 << 30, raybuf_words=32 << 20, max_frames_per_batch=16, max_inflight=3,
-                     max_samples=2048, plain=plain)
+    plain = mode == "plain"
+    srv = _server(rle, mode, hbm_budget_bytes=16 << 30, raybuf_words=32 << 20, max_frames_per_batch=16,
+                  max_inflight=3, max_samples=2048)
     for s, _, _ in pairs:
         srv.add_scene(s)
     rng = np.random.default_rng(20261205)
@@ -285,7 +297,7 @@ def test_config4_mix_against_oracle(rle, po, torch_cuda, plain):
         assert st.batches < 40
     for i, ((sid, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
         gc, gd = c.cpu().numpy().view(np.uint32), d.cpu().numpy()
-        label = f"request {i} (scene {sid}, {view.width}x{view.height}, {'plain' if plain else 'batched'})"
+        label = f"request {i} (scene {sid}, {view.width}x{view.height}, {mode})"
         assert_screen_equal((gc, gd, None), oracle_screen(po, rle, pairs[sid][1], cam, view, hits=False),
                             label + " vs oracle")
         wc, wd = _alone(rle, torch, pairs[sid][0], cam, view)
