@@ -267,13 +267,12 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
             if (st == RLE_OK) st = rle::launch_resolve(sp[i], b->workers[i % k]);
         }
         // joined even after a failed launch: the caller's stream never runs
-        // ahead of work already queued
+        // ahead of work already queued, and the next call waits for it below
         for (int w = 0; w < k; w++) {
             const cudaError_t ej = cudaEventRecord(b->joins[w], b->workers[w]);
             const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(stream, b->joins[w], 0) : ej;
             if (ew != cudaSuccess && st == RLE_OK) st = cuda_fail(ew, "rle_batch_render: join of the worker streams");
         }
-        if (st != RLE_OK) return st;
     } else if (b->tuning.use_graph) {
         if (!b->graph[par]) {
             cudaGraph_t g = nullptr;
@@ -294,13 +293,14 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
     } else {
         st = enqueue(b, par, stream);
-        if (st != RLE_OK) return st;
     }
+    // recorded also after a failed launch, whose earlier launches may still
+    // use the ray buffer: the next call's device work waits for them
     const cudaError_t e = cudaEventRecord(b->staged[par], stream);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    if (e != cudaSuccess) return st != RLE_OK ? st : cuda_fail(e, "cudaEventRecord");
     b->staged_used[par] = true;
     b->parity ^= 1;
-    return RLE_OK;
+    return st;
 }
 
 struct DeviceScope {
