@@ -824,9 +824,10 @@ def poll_all(srv, chunk=65536):
 def latency_breakdown(done, late_s):
     """Where the slowest 1% of a pass's requests spent their time (means, ms):
     the load generator's lateness against the planned arrival (host, Python),
-    the wait in the server's queue (submit -> launch), the device time of the
-    launch that carried the request, and the rest of launch -> done (waiting
-    on the device behind the other in-flight launches, completion polling).
+    the wait in the server's queue (submit -> launch), the device time from
+    the start of the batch that carried the request to the end of its frame,
+    and the rest of launch -> done (waiting on the device behind the other
+    in-flight launches, completion polling).
     Also the generator's worst lateness over the whole pass."""
     ok = [c for c in done if c.status == 0]
     if not ok:

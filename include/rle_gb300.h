@@ -426,8 +426,9 @@ typedef struct rle_completion {
     uint64_t ticket;
     rle_status status;
     double submit_s, launch_s, done_s;  /* host monotonic clock, seconds */
-    double gpu_ms;  /* device time of the launch that carried the request (CUDA events
-                       before and after it on the slot's stream); 0 if it never ran */
+    double gpu_ms;  /* device time from the start of the batch that carried the request to
+                       the end of its frame (CUDA events: one on the slot's stream before
+                       the batch, one behind the frame's launches); 0 if it never ran */
 } rle_completion;
 
 typedef struct rle_server_stats {

@@ -226,8 +226,12 @@ rle_status enqueue(rle_batch* b, int parity, cudaStream_t s) {
     return rle::launch_resolve_batch(rs, s);
 }
 
+// frame_done (optional, n events): event i is recorded once frame i's
+// outputs are written -- behind the frame's own launches in per-frame mode,
+// behind the whole batch in persistent mode.
 rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* const* scenes,
-                         const rle_frame_request* frames, int n, cudaStream_t stream) {
+                         const rle_frame_request* frames, int n, cudaStream_t stream,
+                         cudaEvent_t* frame_done = nullptr) {
     const int par = b->parity;
     if (b->staged_used[par]) {
         const cudaError_t e = cudaEventSynchronize(b->staged[par]);
@@ -265,6 +269,8 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
             rp[i].staging = b->tuning.staging;
             st = rle::launch_raycast(rp[i], b->workers[i % k]);
             if (st == RLE_OK) st = rle::launch_resolve(sp[i], b->workers[i % k]);
+            if (st == RLE_OK && frame_done && cudaEventRecord(frame_done[i], b->workers[i % k]) != cudaSuccess)
+                st = cuda_fail(cudaGetLastError(), "rle_batch_render: frame event");
         }
         // joined even after a failed launch: the caller's stream never runs
         // ahead of work already queued, and the next call waits for it below
@@ -293,6 +299,11 @@ rle_status render_locked(rle_batch* b, const rle_scene* scene, const rle_scene* 
         if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
     } else {
         st = enqueue(b, par, stream);
+    }
+    if (!b->tuning.per_frame && st == RLE_OK && frame_done) {
+        for (int i = 0; i < n && st == RLE_OK; i++)
+            if (cudaEventRecord(frame_done[i], stream) != cudaSuccess)
+                st = cuda_fail(cudaGetLastError(), "rle_batch_render: frame event");
     }
     // recorded also after a failed launch, whose earlier launches may still
     // use the ray buffer: the next call's device work waits for them
@@ -433,7 +444,7 @@ extern "C" rle_status rle_batch_render(rle_batch* b, const rle_scene* scene, con
 namespace rle {
 
 rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, const rle_frame_request* frames, int n,
-                               void* stream) {
+                               void* stream, cudaEvent_t* frame_done) {
     if (!b || !scenes || (n > 0 && !frames) || n < 0 || n > b->max_frames) {
         set_error("rle_batch_render: batch, scenes and 0..max_frames frames required");
         return RLE_ERR_INVALID_ARG;
@@ -441,7 +452,7 @@ rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, con
     if (n == 0) return RLE_OK;
     std::lock_guard<std::mutex> lock(b->mu);
     DeviceScope ds(b->device);
-    return render_locked(b, nullptr, scenes, frames, n, static_cast<cudaStream_t>(stream));
+    return render_locked(b, nullptr, scenes, frames, n, static_cast<cudaStream_t>(stream), frame_done);
 }
 
 size_t batch_capacity_words(const rle_batch* b) { return b ? b->raybuf_words : 0; }

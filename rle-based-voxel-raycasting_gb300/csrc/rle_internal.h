@@ -1,6 +1,7 @@
 // Internal declarations shared by the host C++ and the CUDA translation units.
 #pragma once
 
+#include <cuda_runtime_api.h>
 #include <vector_types.h>
 
 #include "scenegen_math.h"
@@ -166,8 +167,11 @@ rle_status launch_resolve_batch(const BatchResolve& b, void* stream);
 int resolve_batch_blocks(int width, int height);  // 256-pixel blocks of one frame
 
 // A batch whose frames may come from different scenes (one per frame).
+// frame_done (optional, n events): event i is recorded once frame i's outputs
+// are written (per-frame mode: behind its own launches; persistent: behind
+// the batch).
 rle_status batch_render_scenes(rle_batch* b, const rle_scene* const* scenes, const rle_frame_request* frames, int n,
-                               void* stream);
+                               void* stream, cudaEvent_t* frame_done = nullptr);
 size_t batch_capacity_words(const rle_batch* b);
 int batch_max_frames(const rle_batch* b);
 rle_status batch_grid_blocks(int lanes, int threads, int max_samples, bool hits, int staging, int* blocks);

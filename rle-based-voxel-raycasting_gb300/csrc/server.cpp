@@ -4,9 +4,11 @@
 // The scheduler keeps up to max_inflight batch slots busy.  Whenever a slot
 // is free it takes queued requests in arrival order, as many as fit the
 // slot's frame count and ray-buffer words, and launches them as one batch
-// (rle_batch: persistent raycast + resolve from a captured graph) on the
-// slot's stream; completion is observed by polling the slot's event, so no
-// host thread blocks on the device.  Requests that arrive while batches run
+// (rle_batch) on the slot's stream.  Each request completes when its own
+// frame's event does (in the batch's default per-frame mode a frame is done
+// behind its own two launches, before the rest of its batch), and the slot
+// is free again once the whole batch is; both are observed by polling
+// events, so no host thread blocks on the device.  Requests that arrive while batches run
 // simply wait for the next free slot, and batches in different slots overlap
 // on the device.  In `plain` mode each request is its own launch
 // (rle_render_frame) and runs alone, the baseline the batching is measured
@@ -40,7 +42,7 @@ struct Req {
     size_t words = 0;
     double pixels = 0;
     double submit_s = 0, launch_s = 0, done_s = 0;
-    double gpu_ms = 0;  // device time of the request's batch (events around its launches)
+    double gpu_ms = 0;  // device time from its batch's start to the end of its frame (events)
     rle_status status = RLE_OK;
     int state = kQueued;
 };
@@ -50,6 +52,8 @@ struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t start = nullptr;  // recorded before a batch's launches
     cudaEvent_t done = nullptr;   // and after them
+    std::vector<cudaEvent_t> frame_done;  // per frame of the batch (batched mode)
+    std::vector<char> finished;           // per ticket: its completion is out
     bool busy = false;
     std::vector<uint64_t> tickets;
     void* workspace = nullptr;  // plain mode
@@ -107,26 +111,46 @@ void finish(rle_server* s, Req& q, rle_status st, double t) {
     }
 }
 
-// Marks the requests of finished slots done.  Called with the lock held.
+// Completes one request of a slot (lock held).
+void finish_ticket(rle_server* s, Slot& sl, size_t i, cudaEvent_t end, cudaError_t e, double t) {
+    sl.finished[i] = 1;
+    auto it = s->reqs.find(sl.tickets[i]);
+    if (it == s->reqs.end()) return;
+    if (e != cudaSuccess) rle::set_error("server: batch failed on the device: %s", cudaGetErrorString(e));
+    float gpu_ms = 0;
+    if (e == cudaSuccess && cudaEventElapsedTime(&gpu_ms, sl.start, end) != cudaSuccess) gpu_ms = 0;
+    it->second.gpu_ms = gpu_ms;
+    finish(s, it->second, e == cudaSuccess ? RLE_OK : RLE_ERR_CUDA, t);
+}
+
+// Marks done the requests whose frames are finished, and frees the slots
+// whose batches are.  Called with the lock held.  A slot's frames finish
+// roughly in order (frame i runs on the batch's worker stream i mod 8), so
+// the scan of a slot stops after eight frames that are not ready yet.
 bool retire(rle_server* s) {
     bool any = false;
     for (Slot& sl : s->slots) {
         if (!sl.busy) continue;
+        if (!sl.frame_done.empty()) {
+            int pending = 0;
+            for (size_t i = 0; i < sl.tickets.size() && pending < 8; i++) {
+                if (sl.finished[i]) continue;
+                const cudaError_t e = cudaEventQuery(sl.frame_done[i]);
+                if (e == cudaErrorNotReady) {
+                    pending++;
+                    continue;
+                }
+                finish_ticket(s, sl, i, sl.frame_done[i], e, now_s());
+                any = true;
+            }
+        }
         const cudaError_t e = cudaEventQuery(sl.done);
         if (e == cudaErrorNotReady) continue;
         const double t = now_s();
-        const rle_status st = e == cudaSuccess ? RLE_OK : RLE_ERR_CUDA;
-        if (e != cudaSuccess) rle::set_error("server: batch failed on the device: %s", cudaGetErrorString(e));
-        float gpu_ms = 0;
-        if (e == cudaSuccess && cudaEventElapsedTime(&gpu_ms, sl.start, sl.done) != cudaSuccess) gpu_ms = 0;
-        for (uint64_t tk : sl.tickets) {
-            auto it = s->reqs.find(tk);
-            if (it != s->reqs.end()) {
-                it->second.gpu_ms = gpu_ms;
-                finish(s, it->second, st, t);
-            }
-        }
+        for (size_t i = 0; i < sl.tickets.size(); i++)
+            if (!sl.finished[i]) finish_ticket(s, sl, i, sl.done, e, t);
         sl.tickets.clear();
+        sl.finished.clear();
         sl.busy = false;
         any = true;
     }
@@ -181,6 +205,7 @@ bool launch_one(rle_server* s, std::unique_lock<std::mutex>& lk) {
     if (inject) s->inject--;
     slot->busy = true;  // reserve the slot while the lock is dropped
     slot->tickets = take;
+    slot->finished.assign(take.size(), 0);
     s->batches++;
     lk.unlock();
     rle_status st = RLE_OK;
@@ -195,7 +220,7 @@ bool launch_one(rle_server* s, std::unique_lock<std::mutex>& lk) {
                               frames[0].d_colour, frames[0].d_depth, nullptr, slot->stream);
     } else {
         st = rle::batch_render_scenes(slot->batch, scenes.data(), frames.data(), static_cast<int>(frames.size()),
-                                      slot->stream);
+                                      slot->stream, slot->frame_done.data());
     }
     if (st == RLE_OK && cudaEventRecord(slot->done, slot->stream) != cudaSuccess) st = RLE_ERR_CUDA;
     lk.lock();
@@ -203,6 +228,7 @@ bool launch_one(rle_server* s, std::unique_lock<std::mutex>& lk) {
         const double tf = now_s();
         for (uint64_t tk : slot->tickets) finish(s, s->reqs[tk], st, tf);
         slot->tickets.clear();
+        slot->finished.clear();
         slot->busy = false;
         s->cv_done.notify_all();
     }
@@ -248,6 +274,7 @@ void release(rle_server* s) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.batch) rle_batch_free(sl.batch);
         if (sl.done) cudaEventDestroy(sl.done);
+        for (cudaEvent_t ev : sl.frame_done) cudaEventDestroy(ev);
         if (sl.start) cudaEventDestroy(sl.start);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.workspace) cudaFree(sl.workspace);
@@ -310,6 +337,11 @@ extern "C" rle_status rle_server_create(const rle_server_config* cfg, rle_server
                                   &sl.batch);
             if (st == RLE_OK && cfg->batch_tuning.lanes_per_ray != 0)
                 st = rle_batch_set_tuning(sl.batch, &cfg->batch_tuning);
+            for (int i = 0; i < cfg->max_frames_per_batch && st == RLE_OK; i++) {
+                cudaEvent_t ev = nullptr;
+                if (cudaEventCreate(&ev) != cudaSuccess) st = RLE_ERR_CUDA;
+                else sl.frame_done.push_back(ev);
+            }
         }
     }
     if (prev >= 0) cudaSetDevice(prev);
