@@ -305,3 +305,38 @@ def test_config4_mix_against_oracle(rle, po, torch_cuda, mode):
     srv.destroy()
     for s, _, _ in pairs:
         s.free()
+
+
+def test_requests_complete_with_their_own_frame(rle, po, scene_pairs, torch_cuda):
+    """Seven 256x256 requests and then a 1920x1080 one taken into one batch
+    (the server paused while they queue): in the default per-frame mode
+    each request completes with its own frame, so the small frames' device
+    times (batch start -> end of the frame) are shorter than the large
+    frame's, launched last, instead of all being the batch's; every result
+    equals the request rendered alone."""
+    torch = torch_cuda
+    scene = scene_pairs[0][0]
+    srv = rle.Server(hbm_budget_bytes=8 << 30, raybuf_words=32 << 20, max_frames_per_batch=8, max_inflight=1,
+                     max_samples=2048)
+    sid = srv.add_scene(scene)
+    base = _requests(rle, [scene], 8, 33)
+    reqs = [(sid, cam, rle.view_params(256, 256, mip_distance=64)) for _, cam, _ in base[:7]]
+    reqs.append((sid, base[7][1], rle.view_params(1920, 1080, mip_distance=64)))
+    bufs = _buffers(torch, reqs)
+    torch.cuda.synchronize()
+    srv.pause(True)
+    tickets = [srv.submit(s, cam, view, c, d) for (s, cam, view), (c, d) in zip(reqs, bufs)]
+    srv.pause(False)
+    done = {t: srv.wait(t, 20000) for t in tickets}
+    assert all(c.status == 0 for c in done.values())
+    assert srv.stats().batches == 1
+    small = [done[t].gpu_ms for t in tickets[:7]]
+    big = done[tickets[7]].gpu_ms
+    assert 0 < min(small) < big, (small, big)
+    srv.drain(20000)
+    torch.cuda.synchronize()
+    for i, ((s, cam, view), (c, d)) in enumerate(zip(reqs, bufs)):
+        wc, wd = _alone(rle, torch, scene, cam, view)
+        assert np.array_equal(c.cpu().numpy().view(np.uint32), wc), f"request {i} colour"
+        assert np.array_equal(d.cpu().numpy().view(np.uint32), wd.view(np.uint32)), f"request {i} depth"
+    srv.destroy()
