@@ -339,8 +339,12 @@ extern "C" rle_status rle_server_create(const rle_server_config* cfg, rle_server
                 st = rle_batch_set_tuning(sl.batch, &cfg->batch_tuning);
             for (int i = 0; i < cfg->max_frames_per_batch && st == RLE_OK; i++) {
                 cudaEvent_t ev = nullptr;
-                if (cudaEventCreate(&ev) != cudaSuccess) st = RLE_ERR_CUDA;
-                else sl.frame_done.push_back(ev);
+                if (cudaEventCreate(&ev) != cudaSuccess) {
+                    rle::set_error("rle_server_create: cudaEventCreate failed for the per-frame events");
+                    st = RLE_ERR_CUDA;
+                } else {
+                    sl.frame_done.push_back(ev);
+                }
             }
         }
     }
