@@ -60,7 +60,7 @@ def load_rle():
 # default run, captured with ncu (profiles/raycast_traffic_1080p_cave2048.md
 # gives the command and the per-frame figures).  A profiler run cannot be part
 # of the timed benchmark; the capture is repeated when the kernel changes.
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 33_842_586
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 33_878_784
 RAYCAST_DRAM_FRAMES = "frames 0-4 of the timed camera path (seed 20261203, after 5 warm-up frames)"
 # The end-to-end loop renders like a throughput-oriented renderer: several frames in flight (one
 # stream, workspace and output set each) and 16 lanes per column ray (two rays per warp, twice the
